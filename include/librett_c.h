@@ -1,0 +1,106 @@
+/*
+ * librett_c.h -- C-ABI (extern "C") surface of the GB300 tensor-transpose
+ * engine, for FFI callers (ctypes, cffi, cgo, JNI ...).  Plain pointers and
+ * sizes only; the stream is an opaque `void*` holding a cudaStream_t (NULL is
+ * the legacy default stream).  Every function returns a librettResult value
+ * (0 = LIBRETT_SUCCESS) as an int.
+ *
+ * Each entry point is a thin wrapper over the C++ interface in librett.h,
+ * which mirrors LibreTT's src/librett.h; the citation on each line names the
+ * LibreTT declaration it replaces.
+ */
+#ifndef LIBRETT_C_H
+#define LIBRETT_C_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef LIBRETT_H
+typedef unsigned int librettHandle;
+#endif
+
+/* Transpose methods; numbering follows LibreTT src/plan.h:54-56. */
+enum {
+  LIBRETT_METHOD_UNKNOWN = 0,
+  LIBRETT_METHOD_TRIVIAL = 1,      /* fused rank 1: plain copy                    */
+  LIBRETT_METHOD_PACKED = 2,       /* whole Mm u Mk sub-volume per tile           */
+  LIBRETT_METHOD_PACKED_SPLIT = 3, /* as Packed with one rank cut into chunks     */
+  LIBRETT_METHOD_TILED = 4,        /* 2-rank tile of (in rank 0) x (out rank 0)   */
+  LIBRETT_METHOD_TILED_COPY = 5    /* leading rank shared: strided row copy       */
+};
+
+/* Description of a plan: what the planner chose and why. */
+typedef struct librett_plan_info {
+  int method;                      /* LIBRETT_METHOD_*                            */
+  int element_bytes;               /* sizeofType                                  */
+  int fused_rank;                  /* rank after dropping unit dims and fusing    */
+  int fused_perm[16];              /* permutation of the fused problem            */
+  long long fused_dim[16];         /* dims of the fused problem (input order)     */
+  long long tile_extent[16];       /* per fused rank: extent covered by one tile  */
+  long long volume;                /* elements                                    */
+  long long num_tiles;             /* tiles (or rows / chunks) per launch         */
+  int threads;                     /* threads per CTA                             */
+  int slots;                       /* elements (or units) per thread per tile     */
+  int smem_bytes;                  /* dynamic shared memory per CTA               */
+  int pad_shift;                   /* smem padding: 1 element per 2^pad_shift    */
+  int unit_in_bytes;               /* global load width                           */
+  int unit_out_bytes;              /* global store width                          */
+  int run_in_bytes;                /* contiguous input run per tile               */
+  int run_out_bytes;               /* contiguous output run per tile              */
+  int grid;                        /* CTAs launched (0 if not yet known)          */
+  int candidate;                   /* index into the planner's candidate list     */
+  int num_candidates;              /* candidates the planner enumerated           */
+  double model_cost;               /* analytic cost estimate (arbitrary units)    */
+} librett_plan_info;
+
+/* librettInitialize / librettFinalize (LibreTT src/librett.h:57,62). */
+void librett_c_initialize(void);
+void librett_c_finalize(void);
+
+/* librettPlan (LibreTT src/librett.h:78). */
+int librett_c_plan(librettHandle* handle, int rank, const int* dim, const int* permutation,
+                   size_t sizeofType, void* stream);
+
+/* librettPlanMeasure (LibreTT src/librett.h:96-97). Overwrites odata. */
+int librett_c_plan_measure(librettHandle* handle, int rank, const int* dim,
+                           const int* permutation, size_t sizeofType, void* stream,
+                           const void* idata, void* odata);
+
+/* librettExecute (LibreTT src/librett.h:121). Asynchronous on the plan's stream. */
+int librett_c_execute(librettHandle handle, const void* idata, void* odata);
+
+/* librettDestroy (LibreTT src/librett.h:108). */
+int librett_c_destroy(librettHandle handle);
+
+/* Plan introspection; no LibreTT counterpart (LibreTT prints it with
+ * librettPlan_t::print, src/plan.cpp:825-833). */
+int librett_c_plan_info(librettHandle handle, librett_plan_info* info);
+
+/* Host-only planning without a device or a handle: runs the same input check,
+ * rank fusion and tile choice as librett_c_plan for a device with `num_sms`
+ * SMs.  candidate < 0 picks the planner's default; otherwise the numbered
+ * candidate.  No LibreTT counterpart (used by tests and tools). */
+int librett_c_describe(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                       int num_sms, int candidate, librett_plan_info* info);
+
+/* Create a plan using a specific candidate (index as in librett_plan_info).
+ * No LibreTT counterpart; used by autotuning and by plan-choice studies. */
+int librett_c_plan_candidate(librettHandle* handle, int rank, const int* dim,
+                             const int* permutation, size_t sizeofType, void* stream,
+                             int candidate);
+
+/* Number of device kernel launches this library issued since load (all
+ * threads, all devices).  Used to count launches inside a timed region. */
+unsigned long long librett_c_launch_count(void);
+
+/* Human-readable name of a result code. */
+const char* librett_c_result_string(int result);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBRETT_C_H */

@@ -1,0 +1,165 @@
+"""GB300-native tensor-transpose engine with LibreTT's plan-then-execute API.
+
+The engine is the C++/CUDA library ``librett.so`` (include/librett.h for C++
+callers, include/librett_c.h for FFI callers).  This package is a thin
+Python mirror of that interface over ctypes, used by the tests and the
+benchmark:
+
+* ``librettPlan``, ``librettPlanMeasure``, ``librettExecute``,
+  ``librettDestroy``, ``librettInitialize``, ``librettFinalize`` keep LibreTT's
+  names, argument meaning and result codes (src/librett.h:57-121 of LibreTT);
+  where C returns the handle through a pointer these return
+  ``(result, handle)``.
+* ``Plan`` wraps a handle and raises ``LibrettError`` on any non-success code.
+
+Device buffers are passed as integer addresses (``tensor.data_ptr()``) and
+streams as integer ``cudaStream_t`` values (``torch.cuda.Stream.cuda_stream``).
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import _lib
+from ._lib import PlanInfo
+
+LIBRETT_SUCCESS = 0
+LIBRETT_INVALID_PLAN = 1
+LIBRETT_INVALID_PARAMETER = 2
+LIBRETT_INVALID_DEVICE = 3
+LIBRETT_INTERNAL_ERROR = 4
+LIBRETT_UNDEFINED_ERROR = 5
+
+METHOD_NAMES = {0: "Unknown", 1: "Trivial", 2: "Packed", 3: "PackedSplit", 4: "Tiled",
+                5: "TiledCopy"}
+
+
+class LibrettError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        name = _lib.load().librett_c_result_string(code).decode()
+        super().__init__(f"{what}: {name}" if what else name)
+
+
+def _stream(stream) -> int | None:
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return int(stream.cuda_stream)
+    return int(stream)
+
+
+def librettInitialize() -> None:
+    _lib.load().librett_c_initialize()
+
+
+def librettFinalize() -> None:
+    _lib.load().librett_c_finalize()
+
+
+def librettPlan(dim, permutation, sizeofType: int, stream=None) -> tuple[int, int]:
+    """LibreTT librettPlan (src/librett.h:78).  Returns (result, handle)."""
+    h = ctypes.c_uint(0)
+    rc = _lib.load().librett_c_plan(ctypes.byref(h), len(dim), _lib.int_array(dim),
+                                    _lib.int_array(permutation), sizeofType, _stream(stream))
+    return rc, h.value
+
+
+def librettPlanMeasure(dim, permutation, sizeofType: int, stream, idata: int,
+                       odata: int) -> tuple[int, int]:
+    """LibreTT librettPlanMeasure (src/librett.h:96-97).  Overwrites odata."""
+    h = ctypes.c_uint(0)
+    rc = _lib.load().librett_c_plan_measure(ctypes.byref(h), len(dim), _lib.int_array(dim),
+                                            _lib.int_array(permutation), sizeofType,
+                                            _stream(stream), idata, odata)
+    return rc, h.value
+
+
+def librettPlanCandidate(dim, permutation, sizeofType: int, stream,
+                         candidate: int) -> tuple[int, int]:
+    """Plan with one numbered candidate of the planner (no LibreTT counterpart)."""
+    h = ctypes.c_uint(0)
+    rc = _lib.load().librett_c_plan_candidate(ctypes.byref(h), len(dim), _lib.int_array(dim),
+                                              _lib.int_array(permutation), sizeofType,
+                                              _stream(stream), candidate)
+    return rc, h.value
+
+
+def librettExecute(handle: int, idata: int, odata: int) -> int:
+    """LibreTT librettExecute (src/librett.h:121)."""
+    return _lib.load().librett_c_execute(handle, idata, odata)
+
+
+def librettDestroy(handle: int) -> int:
+    """LibreTT librettDestroy (src/librett.h:108)."""
+    return _lib.load().librett_c_destroy(handle)
+
+
+def plan_info(handle: int) -> dict:
+    info = PlanInfo()
+    rc = _lib.load().librett_c_plan_info(handle, ctypes.byref(info))
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_plan_info")
+    return info.as_dict()
+
+
+def describe(dim, permutation, sizeofType: int, num_sms: int = 152,
+             candidate: int = -1) -> dict:
+    """Host-only planning (no device needed): what librettPlan would choose."""
+    info = PlanInfo()
+    rc = _lib.load().librett_c_describe(len(dim), _lib.int_array(dim),
+                                        _lib.int_array(permutation), sizeofType, num_sms,
+                                        candidate, ctypes.byref(info))
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_describe")
+    return info.as_dict()
+
+
+def launch_count() -> int:
+    return int(_lib.load().librett_c_launch_count())
+
+
+class Plan:
+    """Owning wrapper of a plan handle."""
+
+    def __init__(self, dim, permutation, sizeofType: int, stream=None, *,
+                 measure: tuple[int, int] | None = None, candidate: int | None = None):
+        self.dim = [int(d) for d in dim]
+        self.permutation = [int(p) for p in permutation]
+        self.sizeofType = int(sizeofType)
+        if measure is not None:
+            rc, h = librettPlanMeasure(dim, permutation, sizeofType, stream, *measure)
+        elif candidate is not None:
+            rc, h = librettPlanCandidate(dim, permutation, sizeofType, stream, candidate)
+        else:
+            rc, h = librettPlan(dim, permutation, sizeofType, stream)
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librettPlan")
+        self.handle = h
+
+    def execute(self, idata: int, odata: int) -> None:
+        rc = librettExecute(self.handle, idata, odata)
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librettExecute")
+
+    def info(self) -> dict:
+        return plan_info(self.handle)
+
+    def destroy(self) -> None:
+        if self.handle is not None:
+            rc = librettDestroy(self.handle)
+            self.handle = None
+            if rc != LIBRETT_SUCCESS:
+                raise LibrettError(rc, "librettDestroy")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None) is not None:
+                librettDestroy(self.handle)
+        except Exception:
+            pass

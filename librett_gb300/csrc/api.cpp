@@ -1,0 +1,308 @@
+// Public interface: the librett.h C++ functions (same signatures and mangled
+// names as LibreTT's src/librett.h) and the librett_c.h extern "C" wrappers.
+//
+// LibreTT counterparts: src/librett.cpp:45-49 (handle table), :57-83
+// (getDeviceProp), :85-108 (input check), :110-222 (librettPlan), :224-343
+// (librettPlanMeasure), :351-370 (librettDestroy), :372-385 (librettExecute).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <shared_mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "launch.h"
+#include "librett.h"
+#include "librett_c.h"
+#include "plan.h"
+
+namespace lt {
+extern std::atomic<unsigned long long> gLaunchCount;
+}
+
+namespace {
+
+struct PlanObj {
+  lt::PlanDesc pd;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int numSMs = 0;
+  int lastGrid = 0;
+};
+
+// Plans are held by shared_ptr so that an execute that has looked a plan up
+// keeps it alive while a concurrent destroy removes it from the table.  The
+// table lock is not held during the launch (LibreTT holds its mutex across
+// the launch, src/librett.cpp:375).
+std::shared_mutex gPlanMu;
+std::unordered_map<librettHandle, std::shared_ptr<PlanObj>> gPlans;
+std::atomic<librettHandle> gNextHandle{0};
+
+std::mutex gDevMu;
+std::unordered_map<int, int> gDevSMs;
+
+bool currentDevice(int& dev, int& sms) {
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lk(gDevMu);
+  auto it = gDevSMs.find(dev);
+  if (it != gDevSMs.end()) {
+    sms = it->second;
+    return true;
+  }
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
+  gDevSMs[dev] = n;
+  sms = n;
+  return true;
+}
+
+bool aligned(const void* p, size_t esize) {
+  size_t a = esize < 16 ? esize : 16;
+  return ((uintptr_t)p % a) == 0;
+}
+
+librettHandle storePlan(std::shared_ptr<PlanObj> obj) {
+  librettHandle h = gNextHandle.fetch_add(1);
+  std::unique_lock<std::shared_mutex> lk(gPlanMu);
+  gPlans[h] = std::move(obj);
+  return h;
+}
+
+std::shared_ptr<PlanObj> findPlan(librettHandle h) {
+  std::shared_lock<std::shared_mutex> lk(gPlanMu);
+  auto it = gPlans.find(h);
+  if (it == gPlans.end()) return nullptr;
+  return it->second;
+}
+
+void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
+  std::memset(info, 0, sizeof(*info));
+  info->method = pd.method;
+  info->element_bytes = pd.f.esize;
+  info->fused_rank = pd.f.rank;
+  for (int r = 0; r < pd.f.rank; ++r) {
+    info->fused_dim[r] = pd.f.dim[r];
+    info->fused_perm[r] = pd.f.perm[r];
+    info->tile_extent[r] = pd.extent[r];
+  }
+  info->volume = pd.f.vol;
+  info->num_tiles = pd.numWork;
+  info->threads = pd.threads;
+  info->slots = pd.slots;
+  info->smem_bytes = pd.smemBytes;
+  info->pad_shift = pd.padShift;
+  int unit = pd.kernel == lt::K_TILE ? pd.f.esize : pd.unitBytes;
+  info->unit_in_bytes = unit;
+  info->unit_out_bytes = unit;
+  info->run_in_bytes = pd.runInBytes;
+  info->run_out_bytes = pd.runOutBytes;
+  info->grid = grid;
+  info->candidate = pd.candidate;
+  info->num_candidates = pd.numCandidates;
+  info->model_cost = pd.cost;
+}
+
+// Shared by librettPlan and librett_c_plan_candidate: plan with the given
+// candidate (or the heuristic's choice when candidate < 0).
+librettResult planImpl(librettHandle* handle, int rank, const int* dim, const int* perm,
+                       size_t sizeofType, cudaStream_t stream, int candidate) {
+  if (handle == nullptr) return LIBRETT_INVALID_PARAMETER;
+  if (lt::checkInput(rank, dim, perm, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  int dev = 0, sms = 0;
+  if (!currentDevice(dev, sms)) return LIBRETT_INTERNAL_ERROR;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, perm, (int)sizeofType, f);
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
+  int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
+  if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  auto obj = std::make_shared<PlanObj>();
+  obj->pd = cands[pick];
+  obj->stream = stream;
+  obj->device = dev;
+  obj->numSMs = sms;
+  *handle = storePlan(std::move(obj));
+  return LIBRETT_SUCCESS;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// librett.h
+// ---------------------------------------------------------------------------
+
+void librettInitialize() {}
+
+void librettFinalize() {}
+
+librettResult librettPlan(librettHandle* handle, int rank, int* dim, int* permutation,
+                          size_t sizeofType, librett_gpuStream_t& stream) {
+  return planImpl(handle, rank, dim, permutation, sizeofType, stream, -1);
+}
+
+librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int* permutation,
+                                 size_t sizeofType, librett_gpuStream_t& stream, void* idata,
+                                 void* odata) {
+  if (handle == nullptr) return LIBRETT_INVALID_PARAMETER;
+  if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  if (idata == odata || idata == nullptr || odata == nullptr) return LIBRETT_INVALID_PARAMETER;
+  if (!aligned(idata, sizeofType) || !aligned(odata, sizeofType)) return LIBRETT_INVALID_PARAMETER;
+  int dev = 0, sms = 0;
+  if (!currentDevice(dev, sms)) return LIBRETT_INTERNAL_ERROR;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
+  const size_t bytes = (size_t)f.vol * sizeofType;
+  cudaEvent_t ev[2];
+  if (cudaEventCreate(&ev[0]) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return LIBRETT_INTERNAL_ERROR;
+  }
+  // Each candidate: clear the output (as LibreTT does, src/librett.cpp:292),
+  // one untimed warm-up launch, then the best of three timed launches.
+  // LibreTT times a single cold launch per candidate.
+  int best = -1;
+  float bestMs = 0.f;
+  librettResult res = LIBRETT_SUCCESS;
+  for (size_t c = 0; c < cands.size() && res == LIBRETT_SUCCESS; ++c) {
+    int grid = 0;
+    if (cudaMemsetAsync(odata, 0xff, bytes, stream) != cudaSuccess ||
+        lt::launchPlan(cands[c], idata, odata, stream, sms, &grid) != cudaSuccess) {
+      res = LIBRETT_INTERNAL_ERROR;
+      break;
+    }
+    float candMs = -1.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      if (cudaEventRecord(ev[0], stream) != cudaSuccess ||
+          lt::launchPlan(cands[c], idata, odata, stream, sms, &grid) != cudaSuccess ||
+          cudaEventRecord(ev[1], stream) != cudaSuccess || cudaEventSynchronize(ev[1]) != cudaSuccess) {
+        res = LIBRETT_INTERNAL_ERROR;
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[0], ev[1]);
+      if (candMs < 0.f || ms < candMs) candMs = ms;
+    }
+    if (res == LIBRETT_SUCCESS && (best < 0 || candMs < bestMs)) {
+      best = (int)c;
+      bestMs = candMs;
+    }
+  }
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (res != LIBRETT_SUCCESS) return res;
+  auto obj = std::make_shared<PlanObj>();
+  obj->pd = cands[best];
+  obj->stream = stream;
+  obj->device = dev;
+  obj->numSMs = sms;
+  *handle = storePlan(std::move(obj));
+  return LIBRETT_SUCCESS;
+}
+
+librettResult librettDestroy(librettHandle handle) {
+  std::unique_lock<std::shared_mutex> lk(gPlanMu);
+  auto it = gPlans.find(handle);
+  if (it == gPlans.end()) return LIBRETT_INVALID_PLAN;
+  gPlans.erase(it);
+  return LIBRETT_SUCCESS;
+}
+
+librettResult librettExecute(librettHandle handle, void* idata, void* odata) {
+  std::shared_ptr<PlanObj> obj = findPlan(handle);
+  if (!obj) return LIBRETT_INVALID_PLAN;
+  if (idata == odata || idata == nullptr || odata == nullptr) return LIBRETT_INVALID_PARAMETER;
+  if (!aligned(idata, obj->pd.f.esize) || !aligned(odata, obj->pd.f.esize))
+    return LIBRETT_INVALID_PARAMETER;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  if (dev != obj->device) return LIBRETT_INVALID_DEVICE;
+  int grid = 0;
+  if (lt::launchPlan(obj->pd, idata, odata, obj->stream, obj->numSMs, &grid) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
+  obj->lastGrid = grid;
+  return LIBRETT_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// librett_c.h
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+void librett_c_initialize(void) { librettInitialize(); }
+
+void librett_c_finalize(void) { librettFinalize(); }
+
+int librett_c_plan(librettHandle* handle, int rank, const int* dim, const int* permutation,
+                   size_t sizeofType, void* stream) {
+  return planImpl(handle, rank, dim, permutation, sizeofType, (cudaStream_t)stream, -1);
+}
+
+int librett_c_plan_candidate(librettHandle* handle, int rank, const int* dim,
+                             const int* permutation, size_t sizeofType, void* stream,
+                             int candidate) {
+  if (candidate < 0) return LIBRETT_INVALID_PARAMETER;
+  return planImpl(handle, rank, dim, permutation, sizeofType, (cudaStream_t)stream, candidate);
+}
+
+int librett_c_plan_measure(librettHandle* handle, int rank, const int* dim,
+                           const int* permutation, size_t sizeofType, void* stream,
+                           const void* idata, void* odata) {
+  if (dim == nullptr || permutation == nullptr) return LIBRETT_INVALID_PARAMETER;
+  cudaStream_t s = (cudaStream_t)stream;
+  return librettPlanMeasure(handle, rank, const_cast<int*>(dim), const_cast<int*>(permutation),
+                            sizeofType, s, const_cast<void*>(idata), odata);
+}
+
+int librett_c_execute(librettHandle handle, const void* idata, void* odata) {
+  return librettExecute(handle, const_cast<void*>(idata), odata);
+}
+
+int librett_c_destroy(librettHandle handle) { return librettDestroy(handle); }
+
+int librett_c_plan_info(librettHandle handle, librett_plan_info* info) {
+  if (info == nullptr) return LIBRETT_INVALID_PARAMETER;
+  std::shared_ptr<PlanObj> obj = findPlan(handle);
+  if (!obj) return LIBRETT_INVALID_PLAN;
+  fillInfo(obj->pd, obj->lastGrid, info);
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_describe(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                       int num_sms, int candidate, librett_plan_info* info) {
+  if (info == nullptr) return LIBRETT_INVALID_PARAMETER;
+  if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, num_sms > 0 ? num_sms : 152);
+  if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
+  int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
+  if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  fillInfo(cands[pick], 0, info);
+  return LIBRETT_SUCCESS;
+}
+
+unsigned long long librett_c_launch_count(void) {
+  return lt::gLaunchCount.load(std::memory_order_relaxed);
+}
+
+const char* librett_c_result_string(int result) {
+  switch (result) {
+    case LIBRETT_SUCCESS: return "LIBRETT_SUCCESS";
+    case LIBRETT_INVALID_PLAN: return "LIBRETT_INVALID_PLAN";
+    case LIBRETT_INVALID_PARAMETER: return "LIBRETT_INVALID_PARAMETER";
+    case LIBRETT_INVALID_DEVICE: return "LIBRETT_INVALID_DEVICE";
+    case LIBRETT_INTERNAL_ERROR: return "LIBRETT_INTERNAL_ERROR";
+    case LIBRETT_UNDEFINED_ERROR: return "LIBRETT_UNDEFINED_ERROR";
+    default: return "unknown";
+  }
+}
+
+}  // extern "C"

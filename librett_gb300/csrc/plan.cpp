@@ -1,0 +1,569 @@
+// Host planner: input check, rank fusion, candidate enumeration, analytic
+// cost model.  Pure host code (no CUDA runtime calls), so it also runs on
+// machines without a GPU through librett_c_describe.
+//
+// LibreTT counterparts: librettPlanCheckInput (src/librett.cpp:85-108),
+// reduceRanks (src/plan.cpp:64-127), createPlans and the create*Plans family
+// (src/plan.cpp:493-719), countCycles + GpuModel (src/plan.cpp:1073-1643,
+// src/GpuModel.cpp:39-911) and choosePlanHeuristic (src/plan.cpp:778-789).
+// The candidate set and the model are this engine's own: the kernels differ,
+// so the model counts the DRAM sectors and shared-memory wavefronts of this
+// engine's kernels rather than LibreTT's transaction counts.
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <unordered_set>
+
+namespace lt {
+
+int checkInput(int rank, const int* dim, const int* perm, size_t sizeofType) {
+  const int INVALID = 2;  // LIBRETT_INVALID_PARAMETER
+  if (sizeofType != 4 && sizeofType != 8 && sizeofType != 16) return INVALID;
+  if (rank < 1 || rank > MAXR) return INVALID;
+  if (dim == nullptr || perm == nullptr) return INVALID;
+  const int64_t volLimit = int64_t(1) << 40;
+  int64_t vol = 1;
+  for (int i = 0; i < rank; ++i) {
+    if (dim[i] < 1) return INVALID;
+    if (vol > volLimit / dim[i]) return INVALID;
+    vol *= dim[i];
+  }
+  bool seen[MAXR] = {};
+  for (int i = 0; i < rank; ++i) {
+    int p = perm[i];
+    if (p < 0 || p >= rank || seen[p]) return INVALID;
+    seen[p] = true;
+  }
+  return 0;
+}
+
+static void computeStrides(Fused& f) {
+  int64_t s = 1;
+  for (int r = 0; r < f.rank; ++r) {
+    f.sin[r] = s;
+    s *= f.dim[r];
+  }
+  f.vol = s;
+  s = 1;
+  for (int i = 0; i < f.rank; ++i) {
+    f.sout[f.perm[i]] = s;
+    s *= f.dim[f.perm[i]];
+  }
+}
+
+void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f) {
+  std::memset(&f, 0, sizeof(f));
+  f.esize = esize;
+  // 1. Unit dims do not change the layout: drop them.
+  int newIdx[MAXR];
+  int64_t d1[MAXR];
+  int r1 = 0;
+  for (int r = 0; r < rank; ++r) {
+    if (dim[r] > 1) {
+      newIdx[r] = r1;
+      d1[r1++] = dim[r];
+    } else {
+      newIdx[r] = -1;
+    }
+  }
+  if (r1 == 0) {
+    f.rank = 1;
+    f.dim[0] = 1;
+    f.perm[0] = 0;
+    computeStrides(f);
+    return;
+  }
+  int p1[MAXR];
+  int m = 0;
+  for (int i = 0; i < rank; ++i)
+    if (newIdx[perm[i]] >= 0) p1[m++] = newIdx[perm[i]];
+  // 2. Walking the output order, an input rank that directly follows the
+  //    previous one in the input joins its group (it stays adjacent).
+  int gStart[MAXR];
+  int64_t gDim[MAXR];
+  int ng = 0;
+  for (int i = 0; i < r1; ++i) {
+    if (i > 0 && p1[i] == p1[i - 1] + 1) {
+      gDim[ng - 1] *= d1[p1[i]];
+    } else {
+      gStart[ng] = p1[i];
+      gDim[ng] = d1[p1[i]];
+      ++ng;
+    }
+  }
+  // 3. Number the groups by their position in the input.
+  int order[MAXR];
+  for (int g = 0; g < ng; ++g) order[g] = g;
+  std::sort(order, order + ng, [&](int a, int b) { return gStart[a] < gStart[b]; });
+  int inRank[MAXR];
+  for (int k = 0; k < ng; ++k) inRank[order[k]] = k;
+  f.rank = ng;
+  for (int g = 0; g < ng; ++g) {
+    f.dim[inRank[g]] = gDim[g];
+    f.perm[g] = inRank[g];
+  }
+  computeStrides(f);
+}
+
+// ---------------------------------------------------------------------------
+// Tile choice
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct RunInfo {
+  int64_t run;   // contiguous elements
+  int frontier;  // first rank (in that order) not fully inside the tile, -1 if none
+};
+
+RunInfo runOf(const Fused& f, const int64_t* e, bool outputSide) {
+  RunInfo ri{1, -1};
+  for (int i = 0; i < f.rank; ++i) {
+    int r = outputSide ? f.perm[i] : i;
+    ri.run *= e[r];
+    if (e[r] < f.dim[r]) {
+      ri.frontier = r;
+      return ri;
+    }
+  }
+  return ri;
+}
+
+int64_t ceilDiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Relative offsets inside a tile must fit in int32.
+bool offsetsFit(const Fused& f, const int64_t* e) {
+  int64_t si = 0, so = 0;
+  for (int r = 0; r < f.rank; ++r) {
+    si += (e[r] - 1) * f.sin[r];
+    so += (e[r] - 1) * f.sout[r];
+  }
+  return si < (int64_t(1) << 31) && so < (int64_t(1) << 31);
+}
+
+// Greedy growth of the tile until both the input-contiguous and the
+// output-contiguous runs reach `targetElems`, or the tile reaches `maxVol`.
+// The side with the shorter run grows first; a rank that cannot be covered
+// whole is cut into equal chunks so the last chunk is not a sliver.
+void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t* e) {
+  for (int r = 0; r < MAXR; ++r) e[r] = 1;
+  int64_t vol = 1;
+  bool blocked[2] = {false, false};
+  for (int iter = 0; iter < 4 * MAXR + 8; ++iter) {
+    RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
+    bool needIn = ri.run < targetElems && ri.frontier >= 0 && !blocked[0];
+    bool needOut = ro.run < targetElems && ro.frontier >= 0 && !blocked[1];
+    if (!needIn && !needOut) break;
+    int side = (needIn && (!needOut || ri.run <= ro.run)) ? 0 : 1;
+    const RunInfo& rs = side == 0 ? ri : ro;
+    int fr = rs.frontier;
+    int64_t base = rs.run / e[fr];
+    int64_t want = std::max(e[fr] + 1, ceilDiv(targetElems, base));
+    int64_t enew = std::min<int64_t>(f.dim[fr], want);
+    int64_t cap = maxVol / (vol / e[fr]);
+    if (enew > cap) enew = cap;
+    if (enew < f.dim[fr] && enew > e[fr]) {
+      int64_t nch = ceilDiv(f.dim[fr], enew);
+      enew = ceilDiv(f.dim[fr], nch);
+    }
+    if (enew <= e[fr]) {
+      blocked[side] = true;
+      continue;
+    }
+    int64_t old = e[fr];
+    e[fr] = enew;
+    if (!offsetsFit(f, e)) {
+      e[fr] = old;
+      blocked[side] = true;
+      continue;
+    }
+    vol = vol / old * enew;
+  }
+}
+
+}  // namespace
+
+long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
+  const int words = esize / 4;
+  const int lanesPerPhase = 32 / words;
+  const int slots = (tp.tileVol + TILE_THREADS - 1) / TILE_THREADS;
+  long long total = 0;
+  int addr[32];
+  bool act[32];
+  for (int side = 0; side < 2; ++side) {
+    for (int k = 0; k < slots; ++k) {
+      for (int w = 0; w < TILE_THREADS / 32; ++w) {
+        for (int l = 0; l < 32; ++l) {
+          int j = k * TILE_THREADS + w * 32 + l;
+          act[l] = j < tp.tileVol;
+          if (!act[l]) continue;
+          int jj = j;
+          if (side == 1) {
+            int rem = j;
+            jj = 0;
+            for (int i = 0; i < tp.nTR; ++i) {
+              int t = tp.trOut[i];
+              int c = rem % tp.trE[t];
+              rem /= tp.trE[t];
+              jj += c * tp.trInTile[t];
+            }
+          }
+          addr[l] = (jj + (jj >> padShift)) * words;
+        }
+        for (int ph = 0; ph < 32; ph += lanesPerPhase) {
+          // distinct word addresses per bank within the phase
+          int maxPerBank = 0;
+          int cnt[32] = {};
+          int seenWords[32 * 4];
+          int nSeen = 0;
+          for (int l = ph; l < ph + lanesPerPhase; ++l) {
+            if (!act[l]) continue;
+            for (int q = 0; q < words; ++q) {
+              int wa = addr[l] + q;
+              bool dup = false;
+              for (int s = 0; s < nSeen; ++s)
+                if (seenWords[s] == wa) { dup = true; break; }
+              if (dup) continue;
+              seenWords[nSeen++] = wa;
+              int b = wa & 31;
+              if (++cnt[b] > maxPerBank) maxPerBank = cnt[b];
+            }
+          }
+          total += maxPerBank;
+        }
+      }
+    }
+  }
+  return total;
+}
+
+namespace {
+
+int nextPow2(int x) {
+  int p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
+  TileParams& tp = pd.tile;
+  std::memset(&tp, 0, sizeof(tp));
+  int trOfRank[MAXR];
+  int nTR = 0;
+  int64_t vol = 1;
+  for (int r = 0; r < f.rank; ++r) {
+    pd.extent[r] = e[r];
+    vol *= e[r];
+    if (e[r] > 1) {
+      trOfRank[r] = nTR;
+      tp.trE[nTR] = (int)e[r];
+      tp.trSin[nTR] = (int)f.sin[r];
+      tp.trSout[nTR] = (int)f.sout[r];
+      ++nTR;
+    } else {
+      trOfRank[r] = -1;
+    }
+  }
+  if (vol > TILE_MAX_VOL || vol < 1) return false;
+  tp.nTR = nTR;
+  tp.tileVol = (int)vol;
+  int s = 1;
+  for (int t = 0; t < nTR; ++t) {
+    tp.trInTile[t] = s;
+    s *= tp.trE[t];
+  }
+  int k = 0;
+  for (int i = 0; i < f.rank; ++i)
+    if (trOfRank[f.perm[i]] >= 0) tp.trOut[k++] = trOfRank[f.perm[i]];
+  // Grid ranks, decoded in output order so that consecutive tiles write
+  // neighbouring output.
+  int nGR = 0;
+  int64_t numTiles = 1;
+  tp.rgTR[0] = tp.rgTR[1] = -1;
+  for (int i = 0; i < f.rank; ++i) {
+    int r = f.perm[i];
+    int64_t nch = ceilDiv(f.dim[r], e[r]);
+    if (nch <= 1) continue;
+    if (nch >= (int64_t(1) << 31)) return false;
+    tp.grDiv[nGR] = makeFastDiv((uint32_t)nch);
+    tp.grSin[nGR] = e[r] * f.sin[r];
+    tp.grSout[nGR] = e[r] * f.sout[r];
+    tp.grRg[nGR] = -1;
+    if (f.dim[r] % e[r] != 0) {
+      if (tp.nRagged >= 2) return false;
+      int sl = tp.nRagged++;
+      tp.rgTR[sl] = trOfRank[r];
+      tp.rgDim[sl] = f.dim[r];
+      tp.rgE[sl] = (int)e[r];
+      tp.grRg[nGR] = sl;
+    }
+    numTiles *= nch;
+    if (numTiles >= (int64_t(1) << 31)) return false;
+    ++nGR;
+  }
+  tp.nGR = nGR;
+  tp.numTiles = (uint32_t)numTiles;
+  // Padding that minimises shared-memory bank wavefronts.
+  long long best = -1;
+  int bestShift = PAD_NONE;
+  const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
+  for (int sh : shifts) {
+    long long w = smemWavefronts(tp, f.esize, sh);
+    if (best < 0 || w < best) {
+      best = w;
+      bestShift = sh;
+    }
+  }
+  tp.padShift = bestShift;
+  tp.smStride = tp.tileVol + (tp.tileVol >> bestShift);
+  // keep each buffer 16-byte aligned
+  int perVec = 16 / f.esize;
+  if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
+  pd.kernel = K_TILE;
+  pd.threads = TILE_THREADS;
+  pd.slots = nextPow2((tp.tileVol + TILE_THREADS - 1) / TILE_THREADS);
+  pd.ragged = tp.nRagged > 0;
+  pd.smemBytes = 2 * tp.smStride * f.esize;
+  pd.padShift = bestShift;
+  pd.numWork = numTiles;
+  RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
+  pd.runInBytes = (int)std::min<int64_t>(ri.run * f.esize, 1 << 30);
+  pd.runOutBytes = (int)std::min<int64_t>(ro.run * f.esize, 1 << 30);
+  // Method label in LibreTT's terms.
+  int p0 = f.perm[0];
+  bool partial = false;
+  for (int r = 0; r < f.rank; ++r)
+    if (e[r] > 1 && e[r] < f.dim[r]) partial = true;
+  if (nTR == 2 && p0 != 0 && e[0] > 1 && e[p0] > 1)
+    pd.method = Tiled;
+  else if (partial)
+    pd.method = PackedSplit;
+  else
+    pd.method = Packed;
+  return true;
+}
+
+bool buildRows(const Fused& f, int unit, RowParams& rp) {
+  std::memset(&rp, 0, sizeof(rp));
+  int64_t rowBytes = f.dim[0] * f.esize;
+  if (rowBytes % unit != 0) return false;
+  int64_t rowUnits = rowBytes / unit;
+  if (rowUnits >= (int64_t(1) << 31)) return false;
+  rp.rowUnits = (int)rowUnits;
+  int64_t numRows = 1;
+  int n = 0;
+  for (int i = 1; i < f.rank; ++i) {
+    int r = f.perm[i];
+    rp.rDiv[n] = makeFastDiv((uint32_t)f.dim[r]);
+    rp.rSin[n] = f.sin[r] * f.esize / unit;
+    rp.rSout[n] = f.sout[r] * f.esize / unit;
+    numRows *= f.dim[r];
+    if (numRows >= (int64_t(1) << 31)) return false;
+    ++n;
+  }
+  rp.nR = n;
+  rp.numRows = (uint32_t)numRows;
+  int64_t chunks = (rowUnits + 31) / 32;
+  if (numRows * chunks >= (int64_t(1) << 31)) return false;
+  rp.chunkDiv = makeFastDiv((uint32_t)chunks);
+  rp.numItems = (uint32_t)(numRows * chunks);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Analytic model: DRAM sectors touched (sampled over a few tiles), partial
+// sector writes, parallelism and bytes in flight.
+// ---------------------------------------------------------------------------
+
+constexpr double kBandwidth = 6.8e12;   // bytes/s, measured copy ceiling class
+constexpr double kLatency = 1.2e-6;     // s, one load round trip under load
+constexpr double kLaunch = 2.5e-6;      // s, launch + tail
+constexpr int kSmemPerSM = 228 * 1024;
+
+int tileCtasPerSM(const PlanDesc& pd) {
+  int bySmem = kSmemPerSM / (pd.smemBytes + 1024);
+  int regsPerThread = 40 + pd.slots * (5 + pd.f.esize / 4);
+  int byRegs = 65536 / (TILE_THREADS * std::min(regsPerThread, 255));
+  return std::max(1, std::min(std::min(bySmem, byRegs), 2048 / TILE_THREADS));
+}
+
+void decodeTileHost(const TileParams& tp, uint32_t tile, int64_t& bin, int64_t& bout,
+                    int& lim0, int& lim1) {
+  bin = bout = 0;
+  lim0 = lim1 = 1;
+  uint32_t rem = tile;
+  for (int g = 0; g < tp.nGR; ++g) {
+    uint32_t q = fastDivHost(rem, tp.grDiv[g]);
+    uint32_t c = rem - q * tp.grDiv[g].d;
+    rem = q;
+    bin += (int64_t)c * tp.grSin[g];
+    bout += (int64_t)c * tp.grSout[g];
+    int sl = tp.grRg[g];
+    if (sl >= 0) {
+      int lim = (int)std::min<int64_t>(tp.rgE[sl], tp.rgDim[sl] - (int64_t)c * tp.rgE[sl]);
+      if (sl == 0) lim0 = lim; else lim1 = lim;
+    }
+  }
+}
+
+void modelTile(PlanDesc& pd, int numSMs) {
+  const Fused& f = pd.f;
+  const TileParams& tp = pd.tile;
+  int samples = (int)std::min<int64_t>(8, tp.numTiles);
+  double sectorsIn = 0, sectorsOut = 0, partialOut = 0, useful = 0;
+  std::unordered_set<int64_t> si, so;
+  std::vector<int64_t> outCount;
+  for (int s = 0; s < samples; ++s) {
+    uint32_t tile = (uint32_t)((int64_t)s * tp.numTiles / samples);
+    int64_t bin, bout;
+    int lim0, lim1;
+    decodeTileHost(tp, tile, bin, bout, lim0, lim1);
+    si.clear();
+    so.clear();
+    std::unordered_map<int64_t, int> perSector;
+    for (int j = 0; j < tp.tileVol; ++j) {
+      int rem = j;
+      int64_t oi = bin, oo = bout;
+      bool ok = true;
+      for (int t = 0; t < tp.nTR; ++t) {
+        int c = rem % tp.trE[t];
+        rem /= tp.trE[t];
+        oi += (int64_t)c * tp.trSin[t];
+        oo += (int64_t)c * tp.trSout[t];
+        if (t == tp.rgTR[0] && c >= lim0) ok = false;
+        if (t == tp.rgTR[1] && c >= lim1) ok = false;
+      }
+      if (!ok) continue;
+      useful += 1;
+      si.insert(oi * f.esize / 32);
+      int64_t sec = oo * f.esize / 32;
+      so.insert(sec);
+      perSector[sec] += f.esize;
+    }
+    sectorsIn += si.size();
+    sectorsOut += so.size();
+    for (auto& kv : perSector)
+      if (kv.second < 32) partialOut += 1;
+  }
+  double scale = (double)tp.numTiles / samples;
+  double dram = (sectorsIn + sectorsOut + partialOut) * 32.0 * scale;
+  double tDram = dram / kBandwidth;
+  int occ = tileCtasPerSM(pd);
+  double conc = (double)numSMs * occ;
+  double active = std::min<double>(conc, tp.numTiles);
+  double inflight = active * tp.tileVol * f.esize;  // bytes loaded per round
+  double tFlight = (double)f.vol * f.esize / std::max(1.0, inflight) * kLatency;
+  double waves = std::ceil((double)tp.numTiles / conc);
+  double tWaves = waves * 2 * kLatency;
+  // Thread utilisation: slots that carry no element still issue instructions.
+  double util = (double)tp.tileVol / (pd.slots * TILE_THREADS);
+  double tIssue = (double)f.vol * 2.0 / util / (numSMs * 64.0 * 1.9e9);
+  pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
+}
+
+void modelRows(PlanDesc& pd, int numSMs) {
+  const Fused& f = pd.f;
+  int64_t rowBytes = f.dim[0] * f.esize;
+  // Sectors per row averaged over the row start alignments that occur.
+  int64_t rows = f.vol / f.dim[0];
+  int64_t sampleRows = std::min<int64_t>(rows, 64);
+  double secIn = 0, secOut = 0;
+  const RowParams& rp = pd.row;
+  for (int64_t s = 0; s < sampleRows; ++s) {
+    uint32_t row = (uint32_t)(s * rows / sampleRows);
+    int64_t bi = 0, bo = 0;
+    uint32_t rem = row;
+    for (int g = 0; g < rp.nR; ++g) {
+      uint32_t q = fastDivHost(rem, rp.rDiv[g]);
+      uint32_t c = rem - q * rp.rDiv[g].d;
+      rem = q;
+      bi += (int64_t)c * rp.rSin[g];
+      bo += (int64_t)c * rp.rSout[g];
+    }
+    int64_t ai = bi * pd.unitBytes, ao = bo * pd.unitBytes;
+    secIn += (double)((ai + rowBytes - 1) / 32 - ai / 32 + 1);
+    secOut += (double)((ao + rowBytes - 1) / 32 - ao / 32 + 1);
+  }
+  double scale = (double)rows / sampleRows;
+  double tDram = (secIn + secOut) * 32.0 * scale / kBandwidth;
+  double inflight = (double)numSMs * 64 * std::min<int64_t>(rowBytes, 4 * 32 * pd.unitBytes);
+  double tFlight = (double)f.vol * f.esize / inflight * kLatency;
+  pd.cost = std::max(tDram, tFlight) + kLaunch;
+}
+
+}  // namespace
+
+std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
+  std::vector<PlanDesc> out;
+  if (numSMs < 1) numSMs = 1;
+  if (f.rank == 1) {
+    PlanDesc pd;
+    pd.method = Trivial;
+    pd.kernel = K_COPY;
+    pd.f = f;
+    pd.extent[0] = f.dim[0];
+    pd.threads = COPY_THREADS;
+    int64_t bytes = f.vol * f.esize;
+    pd.unitBytes = (bytes % 16 == 0) ? 16 : f.esize;
+    pd.copy.numUnits = bytes / pd.unitBytes;
+    pd.numWork = pd.copy.numUnits;
+    pd.runInBytes = pd.runOutBytes = (int)std::min<int64_t>(bytes, 1 << 30);
+    pd.cost = 2.0 * bytes / kBandwidth + kLaunch;
+    out.push_back(pd);
+  } else {
+    if (f.perm[0] == 0 && f.dim[0] * f.esize >= 128) {
+      PlanDesc pd;
+      pd.method = TiledCopy;
+      pd.kernel = K_ROW;
+      pd.f = f;
+      pd.threads = ROW_THREADS;
+      int64_t rowBytes = f.dim[0] * f.esize;
+      pd.unitBytes = (rowBytes % 16 == 0) ? 16 : f.esize;
+      pd.extent[0] = f.dim[0];
+      for (int r = 1; r < f.rank; ++r) pd.extent[r] = 1;
+      if (buildRows(f, pd.unitBytes, pd.row) && buildRows(f, f.esize, pd.rowScalar)) {
+        pd.numWork = pd.row.numRows;
+        pd.runInBytes = pd.runOutBytes = (int)std::min<int64_t>(rowBytes, 1 << 30);
+        modelRows(pd, numSMs);
+        out.push_back(pd);
+      }
+    }
+    // Tile candidates: (target contiguous run, maximum tile bytes).
+    const int knobs[][2] = {{512, 16384}, {256, 8192}, {128, 4096},  {1024, 32768},
+                            {512, 32768}, {256, 4096}, {2048, 65536}, {64, 2048}};
+    std::vector<std::vector<int64_t>> seen;
+    for (auto& kb : knobs) {
+      int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
+      int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
+      int64_t e[MAXR];
+      chooseExtents(f, target, maxVol, e);
+      std::vector<int64_t> key(e, e + f.rank);
+      if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+      seen.push_back(key);
+      PlanDesc pd;
+      pd.f = f;
+      pd.targetRunBytes = kb[0];
+      pd.maxTileBytes = kb[1];
+      if (!buildTile(f, e, pd)) continue;
+      modelTile(pd, numSMs);
+      out.push_back(pd);
+    }
+  }
+  for (size_t i = 0; i < out.size(); ++i) {
+    out[i].candidate = (int)i;
+    out[i].numCandidates = (int)out.size();
+  }
+  return out;
+}
+
+int chooseHeuristic(const std::vector<PlanDesc>& cands) {
+  int best = 0;
+  for (size_t i = 1; i < cands.size(); ++i)
+    if (cands[i].cost < cands[best].cost) best = (int)i;
+  return best;
+}
+
+}  // namespace lt

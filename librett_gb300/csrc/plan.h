@@ -1,0 +1,152 @@
+// Planner data structures shared by the host planner (plan.cpp), the kernels
+// (kernels.cu) and the API layer (api.cpp).
+//
+// Vocabulary follows LibreTT (src/plan.h:53-118): Mm = ranks contiguous in the
+// input, Mk = ranks contiguous in the output, Mbar = the remaining ranks that
+// the kernels loop over.  Here a plan is described by one "tile": an extent
+// e[r] per fused rank.  Ranks with e[r] > 1 are tile ranks (the Mm u Mk
+// sub-volume one CTA moves through shared memory); ranks with more than one
+// chunk are grid ranks (LibreTT's Mbar, plus the split rank of PackedSplit).
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace lt {
+
+constexpr int MAXR = 16;            // maximum (fused) rank
+constexpr int TILE_THREADS = 256;   // threads per CTA of the tile kernel
+constexpr int TILE_MAX_SLOTS = 16;  // elements per thread per tile (max)
+constexpr int TILE_MAX_VOL = TILE_THREADS * TILE_MAX_SLOTS;
+constexpr int ROW_THREADS = 256;
+constexpr int COPY_THREADS = 256;
+constexpr int PAD_NONE = 31;
+
+// Transpose methods, numbered as LibreTT's enum (src/plan.h:54-56).
+enum Method { Unknown = 0, Trivial = 1, Packed = 2, PackedSplit = 3, Tiled = 4, TiledCopy = 5 };
+
+// Kernel families.
+enum Kernel { K_NONE = 0, K_COPY = 1, K_ROW = 2, K_TILE = 3 };
+
+// Division by an invariant 32-bit divisor for numerators n < 2^31, by the
+// round-up multiply-and-shift method of Granlund and Montgomery ("Division by
+// invariant integers using multiplication", PLDI 1994, Thm 4.2):
+//   l = ceil(log2 d), m = floor(2^(31+l) / d) + 1, q = (n * m) >> (31 + l).
+// Then 2^(31+l) < m*d <= 2^(31+l) + 2^l, which makes q exact for n < 2^31,
+// and m < 2^32 for every 1 <= d <= 2^31.
+struct FastDiv {
+  uint32_t d;
+  uint32_t mul;
+  uint32_t shift;
+};
+
+inline FastDiv makeFastDiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  uint32_t l = 0;
+  while ((1ull << l) < d) ++l;
+  uint64_t m = ((1ull << (31 + l)) / d) + 1;
+  f.mul = (uint32_t)m;
+  f.shift = 31 + l;
+  return f;
+}
+
+inline uint32_t fastDivHost(uint32_t n, const FastDiv& f) {
+  return (uint32_t)(((uint64_t)n * f.mul) >> f.shift);
+}
+
+// Problem after dropping unit dims and fusing ranks that stay adjacent under
+// the permutation (the role of LibreTT's reduceRanks, src/plan.cpp:64-127).
+struct Fused {
+  int rank;           // fused rank (>= 1)
+  int esize;          // element bytes (4, 8, 16)
+  int64_t vol;        // elements
+  int64_t dim[MAXR];  // input order
+  int perm[MAXR];     // output rank i is input rank perm[i]
+  int64_t sin[MAXR];  // input stride of input rank r (elements)
+  int64_t sout[MAXR]; // output stride of input rank r (elements)
+};
+
+// Tile-kernel parameters (passed by value as a __grid_constant__ argument).
+struct TileParams {
+  uint32_t numTiles;
+  int tileVol;          // elements in a full tile
+  int nTR;              // tile ranks (extent > 1), input order
+  int nGR;              // grid ranks (more than one chunk), decode order
+  int padShift;         // smem index = j + (j >> padShift); PAD_NONE = no padding
+  int smStride;         // elements per smem buffer including padding
+  int nRagged;          // ragged ranks (dim not a multiple of extent), <= 2
+  int rgTR[2];          // tile-rank index of each ragged rank
+  long long rgDim[2];   // its full dim
+  int rgE[2];           // its extent
+  int trE[MAXR];        // extent of tile rank t
+  int trInTile[MAXR];   // in-tile input-order stride of tile rank t
+  int trSin[MAXR];      // global input stride of tile rank t (elements)
+  int trSout[MAXR];     // global output stride of tile rank t (elements)
+  int trOut[MAXR];      // tile ranks in output order (indices into tr*)
+  FastDiv grDiv[MAXR];  // number of chunks of grid rank g
+  int grRg[MAXR];       // ragged slot (0/1) of grid rank g, or -1
+  long long grSin[MAXR];  // input step of one chunk of grid rank g
+  long long grSout[MAXR]; // output step of one chunk of grid rank g
+};
+
+// Row-copy parameters (TiledCopy: input rank 0 is also output rank 0).
+struct RowParams {
+  uint32_t numRows;
+  uint32_t numItems;    // numRows * chunks of 32 units (< 2^31)
+  FastDiv chunkDiv;     // chunks of 32 units per row
+  int rowUnits;         // units per row
+  int nR;               // row ranks, decode order (output order)
+  FastDiv rDiv[MAXR];
+  long long rSin[MAXR]; // input stride per row-rank step (units)
+  long long rSout[MAXR];
+};
+
+struct CopyParams {
+  long long numUnits;
+};
+
+// A complete plan: what to launch and with what parameters.
+struct PlanDesc {
+  int method = Unknown;
+  int kernel = K_NONE;
+  Fused f{};
+  int64_t extent[MAXR]{};  // tile extent per fused rank (input order)
+  int threads = 0;
+  int slots = 0;           // tile: elements per thread per tile (template NREG)
+  int ragged = 0;          // tile: has ragged ranks
+  int smemBytes = 0;       // dynamic smem per CTA
+  int unitBytes = 0;       // row/copy: preferred unit (16 when the layout allows)
+  int runInBytes = 0, runOutBytes = 0;
+  int padShift = PAD_NONE;
+  long long numWork = 0;   // tiles / rows / units
+  double cost = 0.0;       // analytic estimate, seconds at nominal bandwidth
+  int candidate = 0;
+  int numCandidates = 0;
+  int targetRunBytes = 0, maxTileBytes = 0;  // knobs that produced the tile
+  TileParams tile{};
+  RowParams row{};         // with unitBytes units
+  RowParams rowScalar{};   // with esize units (misaligned pointers)
+  CopyParams copy{};
+};
+
+// Input validation with LibreTT's rules (src/librett.cpp:85-108) plus the
+// engine's limits (rank <= MAXR, volume <= 2^40).  Returns 0 or 2
+// (LIBRETT_INVALID_PARAMETER).
+int checkInput(int rank, const int* dim, const int* perm, size_t sizeofType);
+
+// Drop unit dims, fuse adjacent ranks, compute strides.
+void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
+
+// Candidate plans for a fused problem on a device with numSMs SMs.  The
+// first entry is never empty.  Each candidate's `cost` is filled in.
+std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
+
+// Index of the candidate the analytic model prefers.
+int chooseHeuristic(const std::vector<PlanDesc>& cands);
+
+// Shared-memory bank wavefronts of one full tile (load-side writes plus
+// store-side reads) for a given padding; exposed for tests.
+long long smemWavefronts(const TileParams& tp, int esize, int padShift);
+
+}  // namespace lt
