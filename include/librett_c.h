@@ -46,6 +46,7 @@ typedef struct librett_plan_info {
   int slots;                       /* elements (or units) per thread per tile     */
   int smem_bytes;                  /* dynamic shared memory per CTA               */
   int pad_shift;                   /* smem padding: 1 element per 2^pad_shift    */
+  int pipeline;                    /* tile: 0 register-staged, 1 cp.async ring   */
   int unit_in_bytes;               /* global load width                           */
   int unit_out_bytes;              /* global store width                          */
   int run_in_bytes;                /* contiguous input run per tile               */

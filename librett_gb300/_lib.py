@@ -31,6 +31,7 @@ class PlanInfo(ctypes.Structure):
         ("slots", ctypes.c_int),
         ("smem_bytes", ctypes.c_int),
         ("pad_shift", ctypes.c_int),
+        ("pipeline", ctypes.c_int),
         ("unit_in_bytes", ctypes.c_int),
         ("unit_out_bytes", ctypes.c_int),
         ("run_in_bytes", ctypes.c_int),
@@ -56,6 +57,7 @@ class PlanInfo(ctypes.Structure):
             "slots": self.slots,
             "smem_bytes": self.smem_bytes,
             "pad_shift": self.pad_shift,
+            "pipeline": self.pipeline,
             "unit_in_bytes": self.unit_in_bytes,
             "unit_out_bytes": self.unit_out_bytes,
             "run_in_bytes": self.run_in_bytes,

@@ -95,6 +95,7 @@ void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   info->slots = pd.slots;
   info->smem_bytes = pd.smemBytes;
   info->pad_shift = pd.padShift;
+  info->pipeline = pd.pipe;
   int unit = pd.kernel == lt::K_TILE ? pd.f.esize : pd.unitBytes;
   info->unit_in_bytes = unit;
   info->unit_out_bytes = unit;

@@ -306,6 +306,22 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
   }
   tp.nGR = nGR;
   tp.numTiles = (uint32_t)numTiles;
+  // Divisors used to recover the coordinate along a ragged rank from an
+  // in-tile index (input order for loads, output order for stores).
+  int outStride[MAXR];
+  {
+    int so = 1;
+    for (int i = 0; i < nTR; ++i) {
+      outStride[tp.trOut[i]] = so;
+      so *= tp.trE[tp.trOut[i]];
+    }
+  }
+  for (int sl = 0; sl < 2; ++sl) {
+    int t = tp.rgTR[sl];
+    tp.rgEDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)tp.trE[t] : 1u);
+    tp.rgInDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)tp.trInTile[t] : 1u);
+    tp.rgOutDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)outStride[t] : 1u);
+  }
   // Padding that minimises shared-memory bank wavefronts.
   long long best = -1;
   int bestShift = PAD_NONE;
@@ -326,7 +342,7 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
   pd.threads = TILE_THREADS;
   pd.slots = nextPow2((tp.tileVol + TILE_THREADS - 1) / TILE_THREADS);
   pd.ragged = tp.nRagged > 0;
-  pd.smemBytes = 2 * tp.smStride * f.esize;
+  pd.smemBytes = (pd.pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
   pd.padShift = bestShift;
   pd.numWork = numTiles;
   RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
@@ -385,7 +401,7 @@ constexpr int kSmemPerSM = 228 * 1024;
 
 int tileCtasPerSM(const PlanDesc& pd) {
   int bySmem = kSmemPerSM / (pd.smemBytes + 1024);
-  int regsPerThread = 40 + pd.slots * (5 + pd.f.esize / 4);
+  int regsPerThread = 32 + pd.slots * 3 + pd.f.esize / 4;
   int byRegs = 65536 / (TILE_THREADS * std::min(regsPerThread, 255));
   return std::max(1, std::min(std::min(bySmem, byRegs), 2048 / TILE_THREADS));
 }
@@ -454,7 +470,8 @@ void modelTile(PlanDesc& pd, int numSMs) {
   int occ = tileCtasPerSM(pd);
   double conc = (double)numSMs * occ;
   double active = std::min<double>(conc, tp.numTiles);
-  double inflight = active * tp.tileVol * f.esize;  // bytes loaded per round
+  int ahead = pd.pipe == PIPE_ASYNC ? TILE_STAGES - 1 : 1;
+  double inflight = active * ahead * tp.tileVol * f.esize;  // loads in flight
   double tFlight = (double)f.vol * f.esize / std::max(1.0, inflight) * kLatency;
   double waves = std::ceil((double)tp.numTiles / conc);
   double tWaves = waves * 2 * kLatency;
@@ -543,13 +560,18 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
       std::vector<int64_t> key(e, e + f.rank);
       if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
       seen.push_back(key);
-      PlanDesc pd;
-      pd.f = f;
-      pd.targetRunBytes = kb[0];
-      pd.maxTileBytes = kb[1];
-      if (!buildTile(f, e, pd)) continue;
-      modelTile(pd, numSMs);
-      out.push_back(pd);
+      for (int pipe : {PIPE_REG, PIPE_ASYNC}) {
+        PlanDesc pd;
+        pd.f = f;
+        pd.pipe = pipe;
+        pd.targetRunBytes = kb[0];
+        pd.maxTileBytes = kb[1];
+        if (!buildTile(f, e, pd)) continue;
+        modelTile(pd, numSMs);
+        // per-element cp.async is slower than plain loads below 16 bytes
+        if (pipe == PIPE_ASYNC && f.esize < 16) pd.cost *= 1.5;
+        out.push_back(pd);
+      }
     }
   }
   for (size_t i = 0; i < out.size(); ++i) {

@@ -21,6 +21,11 @@ constexpr int TILE_MAX_VOL = TILE_THREADS * TILE_MAX_SLOTS;
 constexpr int ROW_THREADS = 256;
 constexpr int COPY_THREADS = 256;
 constexpr int PAD_NONE = 31;
+constexpr int TILE_STAGES = 3;     // cp.async pipeline depth of the tile kernel
+
+// Tile pipelines: register-staged loads (2 shared buffers) or cp.async
+// straight into a TILE_STAGES-deep ring of shared buffers.
+enum Pipe { PIPE_REG = 0, PIPE_ASYNC = 1 };
 
 // Transpose methods, numbered as LibreTT's enum (src/plan.h:54-56).
 enum Method { Unknown = 0, Trivial = 1, Packed = 2, PackedSplit = 3, Tiled = 4, TiledCopy = 5 };
@@ -79,6 +84,9 @@ struct TileParams {
   int rgTR[2];          // tile-rank index of each ragged rank
   long long rgDim[2];   // its full dim
   int rgE[2];           // its extent
+  FastDiv rgEDiv[2];    // division by the extent
+  FastDiv rgInDiv[2];   // by its in-tile input-order stride
+  FastDiv rgOutDiv[2];  // by its in-tile output-order stride
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
@@ -119,6 +127,7 @@ struct PlanDesc {
   int unitBytes = 0;       // row/copy: preferred unit (16 when the layout allows)
   int runInBytes = 0, runOutBytes = 0;
   int padShift = PAD_NONE;
+  int pipe = PIPE_REG;     // tile: Pipe
   long long numWork = 0;   // tiles / rows / units
   double cost = 0.0;       // analytic estimate, seconds at nominal bandwidth
   int candidate = 0;
