@@ -96,9 +96,8 @@ void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   info->smem_bytes = pd.smemBytes;
   info->pad_shift = pd.padShift;
   info->pipeline = pd.pipe;
-  int unit = pd.kernel == lt::K_TILE ? pd.f.esize : pd.unitBytes;
-  info->unit_in_bytes = unit;
-  info->unit_out_bytes = unit;
+  info->unit_in_bytes = pd.unitBytes;
+  info->unit_out_bytes = pd.kernel == lt::K_TILE ? pd.unitOutBytes : pd.unitBytes;
   info->run_in_bytes = pd.runInBytes;
   info->run_out_bytes = pd.runOutBytes;
   info->grid = grid;

@@ -112,10 +112,21 @@ cudaError_t launchPlan(const PlanDesc& pd, const void* in, void* out, cudaStream
       break;
     }
     case K_TILE: {
+      const PlanDesc* use = &pd;
+      PlanDesc scalar;
+      if ((pd.tile.lv > 1 || pd.tile.sv > 1) && align % 16 != 0) {
+        // 16-byte units need 16-byte aligned tensors; fall back to elements
+        scalar = pd;
+        scalar.tile = pd.tileScalar;
+        scalar.slots = pd.slotsScalar;
+        scalar.smemBytes = pd.smemBytesScalar;
+        scalar.pipe = PIPE_REG;
+        use = &scalar;
+      }
       switch (pd.f.esize) {
-        case 4: err = launchTile4(pd, in, out, s, numSMs, &g); break;
-        case 8: err = launchTile8(pd, in, out, s, numSMs, &g); break;
-        case 16: err = launchTile16(pd, in, out, s, numSMs, &g); break;
+        case 4: err = launchTile4(*use, in, out, s, numSMs, &g); break;
+        case 8: err = launchTile8(*use, in, out, s, numSMs, &g); break;
+        case 16: err = launchTile16(*use, in, out, s, numSMs, &g); break;
         default: err = cudaErrorInvalidValue;
       }
       break;

@@ -1,5 +1,5 @@
 // Tile kernel instantiations for 16-byte elements.
-#include "kernels.cuh"
+#include "tile_kernel.cuh"
 #define LT_ES 16
 #define LT_LAUNCH_NAME launchTile16
 #include "tile_launch.inc"

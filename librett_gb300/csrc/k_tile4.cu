@@ -1,5 +1,5 @@
 // Tile kernel instantiations for 4-byte elements.
-#include "kernels.cuh"
+#include "tile_kernel.cuh"
 #define LT_ES 4
 #define LT_LAUNCH_NAME launchTile4
 #include "tile_launch.inc"

@@ -1,5 +1,5 @@
 // Tile kernel instantiations for 8-byte elements.
-#include "kernels.cuh"
+#include "tile_kernel.cuh"
 #define LT_ES 8
 #define LT_LAUNCH_NAME launchTile8
 #include "tile_launch.inc"

@@ -144,6 +144,27 @@ bool offsetsFit(const Fused& f, const int64_t* e) {
   return si < (int64_t(1) << 31) && so < (int64_t(1) << 31);
 }
 
+// Extent for a rank of dim d cut into chunks, at most `want` and more than
+// `cur`: prefer a divisor of d (no ragged last chunk) that is a multiple of
+// the 16-byte unit V when d is, within 60% of `want`; else equal chunks.
+int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
+  int64_t lo = std::max(cur + 1, (want * 3 + 4) / 5);
+  for (int pass = 0; pass < 2; ++pass) {
+    for (int64_t c = want; c >= lo; --c) {
+      if (d % c != 0) continue;
+      if (pass == 0 && V > 1 && d % V == 0 && c % V != 0) continue;
+      return c;
+    }
+  }
+  int64_t nch = ceilDiv(d, want);
+  int64_t e = ceilDiv(d, nch);
+  if (V > 1 && d % V == 0 && e % V != 0) {
+    int64_t up = (e + V - 1) / V * V;
+    if (up <= want) e = up;
+  }
+  return e;
+}
+
 // Greedy growth of the tile until both the input-contiguous and the
 // output-contiguous runs reach `targetElems`, or the tile reaches `maxVol`.
 // The side with the shorter run grows first; a rank that cannot be covered
@@ -165,10 +186,7 @@ void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t*
     int64_t enew = std::min<int64_t>(f.dim[fr], want);
     int64_t cap = maxVol / (vol / e[fr]);
     if (enew > cap) enew = cap;
-    if (enew < f.dim[fr] && enew > e[fr]) {
-      int64_t nch = ceilDiv(f.dim[fr], enew);
-      enew = ceilDiv(f.dim[fr], nch);
-    }
+    if (enew < f.dim[fr] && enew > e[fr]) enew = pickExtent(f.dim[fr], enew, e[fr], 16 / f.esize);
     if (enew <= e[fr]) {
       blocked[side] = true;
       continue;
@@ -187,54 +205,69 @@ void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t*
 }  // namespace
 
 long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
+  // Simulates one full tile: load-side unit writes and, for each element of
+  // a store unit, the store-side element reads.  A phase of lanes covers 128
+  // bytes; its wavefronts are the largest number of distinct 4-byte words
+  // any bank is asked for.
   const int words = esize / 4;
-  const int lanesPerPhase = 32 / words;
-  const int slots = (tp.tileVol + TILE_THREADS - 1) / TILE_THREADS;
+  auto smIdx = [&](int j) { return j + ((j >> padShift) << tp.padLog); };
   long long total = 0;
-  int addr[32];
-  bool act[32];
-  for (int side = 0; side < 2; ++side) {
-    for (int k = 0; k < slots; ++k) {
-      for (int w = 0; w < TILE_THREADS / 32; ++w) {
-        for (int l = 0; l < 32; ++l) {
-          int j = k * TILE_THREADS + w * 32 + l;
-          act[l] = j < tp.tileVol;
-          if (!act[l]) continue;
-          int jj = j;
-          if (side == 1) {
-            int rem = j;
-            jj = 0;
-            for (int i = 0; i < tp.nTR; ++i) {
-              int t = tp.trOut[i];
-              int c = rem % tp.trE[t];
-              rem /= tp.trE[t];
-              jj += c * tp.trInTile[t];
-            }
-          }
-          addr[l] = (jj + (jj >> padShift)) * words;
-        }
-        for (int ph = 0; ph < 32; ph += lanesPerPhase) {
-          // distinct word addresses per bank within the phase
-          int maxPerBank = 0;
-          int cnt[32] = {};
-          int seenWords[32 * 4];
-          int nSeen = 0;
-          for (int l = ph; l < ph + lanesPerPhase; ++l) {
-            if (!act[l]) continue;
-            for (int q = 0; q < words; ++q) {
-              int wa = addr[l] + q;
-              bool dup = false;
-              for (int s = 0; s < nSeen; ++s)
-                if (seenWords[s] == wa) { dup = true; break; }
-              if (dup) continue;
-              seenWords[nSeen++] = wa;
-              int b = wa & 31;
-              if (++cnt[b] > maxPerBank) maxPerBank = cnt[b];
-            }
-          }
-          total += maxPerBank;
+  std::vector<int> jOfQ(tp.tileVol);
+  for (int q = 0; q < tp.tileVol; ++q) {
+    int rem = q, jj = 0;
+    for (int i = 0; i < tp.nTR; ++i) {
+      int t = tp.trOut[i];
+      int c = rem % tp.trE[t];
+      rem /= tp.trE[t];
+      jj += c * tp.trInTile[t];
+    }
+    jOfQ[q] = jj;
+  }
+  auto phaseCost = [&](const int* addr, const bool* act, int lanes, int wordsPerLane) {
+    long long cost = 0;
+    int lanesPerPhase = std::max(1, 32 / wordsPerLane);
+    for (int ph = 0; ph < lanes; ph += lanesPerPhase) {
+      int cnt[32] = {};
+      int maxPerBank = 0;
+      int seen[32 * 4];
+      int nSeen = 0;
+      for (int l = ph; l < std::min(lanes, ph + lanesPerPhase); ++l) {
+        if (!act[l]) continue;
+        for (int q = 0; q < wordsPerLane; ++q) {
+          int wa = addr[l] + q;
+          bool dup = false;
+          for (int s2 = 0; s2 < nSeen; ++s2)
+            if (seen[s2] == wa) { dup = true; break; }
+          if (dup) continue;
+          seen[nSeen++] = wa;
+          int b = wa & 31;
+          if (++cnt[b] > maxPerBank) maxPerBank = cnt[b];
         }
       }
+      cost += maxPerBank;
+    }
+    return cost;
+  };
+  int addr[32];
+  bool act[32];
+  // load side: one unit of lv elements per lane
+  for (int base = 0; base < tp.nIn; base += 32) {
+    for (int l = 0; l < 32; ++l) {
+      int u = base + l;
+      act[l] = u < tp.nIn;
+      addr[l] = act[l] ? smIdx(u * tp.lv) * words : 0;
+    }
+    total += phaseCost(addr, act, 32, words * tp.lv);
+  }
+  // store side: element m of each lane's store unit, one instruction per m
+  for (int base = 0; base < tp.nOut; base += 32) {
+    for (int m = 0; m < tp.sv; ++m) {
+      for (int l = 0; l < 32; ++l) {
+        int w = base + l;
+        act[l] = w < tp.nOut;
+        addr[l] = act[l] ? smIdx(jOfQ[w * tp.sv + m]) * words : 0;
+      }
+      total += phaseCost(addr, act, 32, words);
     }
   }
   return total;
@@ -248,14 +281,60 @@ int nextPow2(int x) {
   return p;
 }
 
-bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
-  TileParams& tp = pd.tile;
+int log2i(int x) {
+  int l = 0;
+  while ((1 << l) < x) ++l;
+  return l;
+}
+
+// Largest unit (elements) that never straddles a run boundary or a partial
+// tile edge and stays 16-byte aligned, for one side (input or output order).
+int unitFor(const Fused& f, const int64_t* e, bool outputSide, const TileParams& tp,
+            const int* trOfRank) {
+  const int V = 16 / f.esize;
+  if (V == 1) return 1;
+  RunInfo ri = runOf(f, e, outputSide);
+  if (ri.run % V != 0) return 1;
+  // dims of the ranks up to the frontier (in that order) must make every
+  // stride beyond the run a multiple of V
+  if (ri.frontier >= 0) {
+    int64_t prefix = 1;
+    for (int i = 0; i < f.rank; ++i) {
+      int r = outputSide ? f.perm[i] : i;
+      prefix *= f.dim[r];
+      if (r == ri.frontier) break;
+    }
+    if (prefix % V != 0) return 1;
+  }
+  // a ragged rank must be constant across a unit, or be the lowest tile
+  // rank with extent and dim multiples of V
+  for (int sl = 0; sl < tp.nRagged; ++sl) {
+    int t = tp.rgTR[sl];
+    int64_t stride = 1;
+    for (int i = 0; i < f.rank; ++i) {
+      int r = outputSide ? f.perm[i] : i;
+      if (trOfRank[r] == t) break;
+      stride *= e[r];
+    }
+    if (stride % V == 0) continue;
+    int r = -1;
+    for (int rr = 0; rr < f.rank; ++rr)
+      if (trOfRank[rr] == t) r = rr;
+    if (stride == 1 && e[r] % V == 0 && f.dim[r] % V == 0) continue;
+    return 1;
+  }
+  return V;
+}
+
+// Fills tp for extents e with the given units; returns false when the tile
+// does not fit the kernel's limits.
+bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe, TileParams& tp,
+                     int& smemBytes) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
   int64_t vol = 1;
   for (int r = 0; r < f.rank; ++r) {
-    pd.extent[r] = e[r];
     vol *= e[r];
     if (e[r] > 1) {
       trOfRank[r] = nTR;
@@ -306,8 +385,6 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
   }
   tp.nGR = nGR;
   tp.numTiles = (uint32_t)numTiles;
-  // Divisors used to recover the coordinate along a ragged rank from an
-  // in-tile index (input order for loads, output order for stores).
   int outStride[MAXR];
   {
     int so = 1;
@@ -322,11 +399,21 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
     tp.rgInDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)tp.trInTile[t] : 1u);
     tp.rgOutDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)outStride[t] : 1u);
   }
+  // Units: requested widths, reduced to 1 where the layout does not allow.
+  if (lv > 1 && unitFor(f, e, false, tp, trOfRank) < lv) lv = 1;
+  if (sv > 1 && unitFor(f, e, true, tp, trOfRank) < sv) sv = 1;
+  if (pipe == PIPE_ASYNC && lv * f.esize != 16) return false;
+  tp.lv = lv;
+  tp.sv = sv;
+  tp.padLog = log2i(lv);
+  tp.nIn = tp.tileVol / lv;
+  tp.nOut = tp.tileVol / sv;
   // Padding that minimises shared-memory bank wavefronts.
   long long best = -1;
   int bestShift = PAD_NONE;
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
+    if (sh < tp.padLog) continue;
     long long w = smemWavefronts(tp, f.esize, sh);
     if (best < 0 || w < best) {
       best = w;
@@ -334,17 +421,35 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
     }
   }
   tp.padShift = bestShift;
-  tp.smStride = tp.tileVol + (tp.tileVol >> bestShift);
-  // keep each buffer 16-byte aligned
+  tp.smStride = tp.tileVol + ((tp.tileVol >> bestShift) << tp.padLog);
   int perVec = 16 / f.esize;
   if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
+  if (tp.smStride + 16 > 65535) return false;  // shared indices are 16-bit
+  const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 +
+                         ((4 * (tp.nIn + tp.nOut) * (tp.nRagged > 0 ? 2 : 1) + 15) / 16) * 16;
+  smemBytes = tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
+  return smemBytes <= 227 * 1024;
+}
+
+bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
+  const int V = 16 / f.esize;
+  int smem = 0, smemScalar = 0;
+  if (!buildTileParams(f, e, V, V, pd.pipe, pd.tile, smem)) return false;
+  // misaligned pointers fall back to element-size units
+  if (!buildTileParams(f, e, 1, 1, PIPE_REG, pd.tileScalar, smemScalar)) return false;
+  const TileParams& tp = pd.tile;
+  for (int r = 0; r < f.rank; ++r) pd.extent[r] = e[r];
   pd.kernel = K_TILE;
   pd.threads = TILE_THREADS;
-  pd.slots = nextPow2((tp.tileVol + TILE_THREADS - 1) / TILE_THREADS);
+  pd.slots = nextPow2((tp.nIn + TILE_THREADS - 1) / TILE_THREADS);
+  pd.slotsScalar = nextPow2((pd.tileScalar.nIn + TILE_THREADS - 1) / TILE_THREADS);
   pd.ragged = tp.nRagged > 0;
-  pd.smemBytes = (pd.pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
-  pd.padShift = bestShift;
-  pd.numWork = numTiles;
+  pd.smemBytes = smem;
+  pd.smemBytesScalar = smemScalar;
+  pd.padShift = tp.padShift;
+  pd.unitBytes = tp.lv * f.esize;
+  pd.unitOutBytes = tp.sv * f.esize;
+  pd.numWork = tp.numTiles;
   RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
   pd.runInBytes = (int)std::min<int64_t>(ri.run * f.esize, 1 << 30);
   pd.runOutBytes = (int)std::min<int64_t>(ro.run * f.esize, 1 << 30);
@@ -353,7 +458,7 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
   bool partial = false;
   for (int r = 0; r < f.rank; ++r)
     if (e[r] > 1 && e[r] < f.dim[r]) partial = true;
-  if (nTR == 2 && p0 != 0 && e[0] > 1 && e[p0] > 1)
+  if (tp.nTR == 2 && p0 != 0 && e[0] > 1 && e[p0] > 1)
     pd.method = Tiled;
   else if (partial)
     pd.method = PackedSplit;
@@ -401,7 +506,7 @@ constexpr int kSmemPerSM = 228 * 1024;
 
 int tileCtasPerSM(const PlanDesc& pd) {
   int bySmem = kSmemPerSM / (pd.smemBytes + 1024);
-  int regsPerThread = 32 + pd.slots * 3 + pd.f.esize / 4;
+  int regsPerThread = 32 + (pd.pipe == PIPE_ASYNC ? 0 : pd.slots * pd.unitBytes / 4);
   int byRegs = 65536 / (TILE_THREADS * std::min(regsPerThread, 255));
   return std::max(1, std::min(std::min(bySmem, byRegs), 2048 / TILE_THREADS));
 }
@@ -476,8 +581,11 @@ void modelTile(PlanDesc& pd, int numSMs) {
   double waves = std::ceil((double)tp.numTiles / conc);
   double tWaves = waves * 2 * kLatency;
   // Thread utilisation: slots that carry no element still issue instructions.
-  double util = (double)tp.tileVol / (pd.slots * TILE_THREADS);
-  double tIssue = (double)f.vol * 2.0 / util / (numSMs * 64.0 * 1.9e9);
+  double util = (double)tp.nIn / (pd.slots * TILE_THREADS);
+  // instructions per element: ~8 per load unit and ~6 + 2 per element of a
+  // store unit, over 4 schedulers x 32 lanes per SM
+  double instPerElem = 8.0 / tp.lv / util + 6.0 / tp.sv + 2.0;
+  double tIssue = (double)f.vol * instPerElem / (numSMs * 128.0 * 1.9e9);
   pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
 }
 
@@ -569,7 +677,7 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
         if (!buildTile(f, e, pd)) continue;
         modelTile(pd, numSMs);
         // per-element cp.async is slower than plain loads below 16 bytes
-        if (pipe == PIPE_ASYNC && f.esize < 16) pd.cost *= 1.5;
+        if (pipe == PIPE_ASYNC && f.esize < 16) pd.cost *= 1.05;
         out.push_back(pd);
       }
     }

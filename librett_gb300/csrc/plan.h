@@ -76,9 +76,14 @@ struct Fused {
 struct TileParams {
   uint32_t numTiles;
   int tileVol;          // elements in a full tile
+  int lv;               // elements per load unit (16-byte units when > 1)
+  int sv;               // elements per store unit
+  int padLog;           // log2(lv): padding comes in whole load units
+  int nIn;              // load units per tile (tileVol / lv)
+  int nOut;             // store units per tile (tileVol / sv)
   int nTR;              // tile ranks (extent > 1), input order
   int nGR;              // grid ranks (more than one chunk), decode order
-  int padShift;         // smem index = j + (j >> padShift); PAD_NONE = no padding
+  int padShift;         // smem index = j + ((j >> padShift) << padLog); PAD_NONE = none
   int smStride;         // elements per smem buffer including padding
   int nRagged;          // ragged ranks (dim not a multiple of extent), <= 2
   int rgTR[2];          // tile-rank index of each ragged rank
@@ -121,7 +126,7 @@ struct PlanDesc {
   Fused f{};
   int64_t extent[MAXR]{};  // tile extent per fused rank (input order)
   int threads = 0;
-  int slots = 0;           // tile: elements per thread per tile (template NREG)
+  int slots = 0;           // tile: load units per thread per tile (template NL)
   int ragged = 0;          // tile: has ragged ranks
   int smemBytes = 0;       // dynamic smem per CTA
   int unitBytes = 0;       // row/copy: preferred unit (16 when the layout allows)
@@ -134,6 +139,9 @@ struct PlanDesc {
   int numCandidates = 0;
   int targetRunBytes = 0, maxTileBytes = 0;  // knobs that produced the tile
   TileParams tile{};
+  TileParams tileScalar{}; // element-size units (misaligned pointers)
+  int slotsScalar = 0, smemBytesScalar = 0;
+  int unitOutBytes = 0;    // tile: store unit bytes
   RowParams row{};         // with unitBytes units
   RowParams rowScalar{};   // with esize units (misaligned pointers)
   CopyParams copy{};

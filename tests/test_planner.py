@@ -43,7 +43,11 @@ def _check_plan(dims, perm, es, candidate=-1):
     # tile kernels: extents, tiles, slots and smem are consistent
     assert all(1 <= e <= d for e, d in zip(ext, fd))
     tvol = int(np.prod(ext))
-    assert tvol <= 4096 and info["slots"] * info["threads"] >= tvol
+    lv = info["unit_in_bytes"] // es
+    sv = info["unit_out_bytes"] // es
+    assert lv in (1, 16 // es) and sv in (1, 16 // es)
+    assert tvol % lv == 0 and tvol % sv == 0
+    assert tvol <= 4096 and info["slots"] * info["threads"] * lv >= tvol
     assert info["slots"] in (1, 2, 4, 8, 16)
     assert info["num_tiles"] == int(np.prod([-(-d // e) for d, e in zip(fd, ext)]))
     assert info["smem_bytes"] <= 227 * 1024
