@@ -169,14 +169,28 @@ int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
 // output-contiguous runs reach `targetElems`, or the tile reaches `maxVol`.
 // The side with the shorter run grows first; a rank that cannot be covered
 // whole is cut into equal chunks so the last chunk is not a sliver.
-void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t* e) {
+void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t fillVol,
+                   int64_t* e) {
   for (int r = 0; r < MAXR; ++r) e[r] = 1;
   int64_t vol = 1;
   bool blocked[2] = {false, false};
-  for (int iter = 0; iter < 4 * MAXR + 8; ++iter) {
+  bool filling = false;
+  for (int iter = 0; iter < 8 * MAXR + 16; ++iter) {
     RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
     bool needIn = ri.run < targetElems && ri.frontier >= 0 && !blocked[0];
     bool needOut = ro.run < targetElems && ro.frontier >= 0 && !blocked[1];
+    if (!needIn && !needOut && !filling && vol < fillVol) {
+      // Both runs are long enough but the tile is small: keep growing the
+      // shorter side (by doubling) until the tile reaches fillVol.
+      filling = true;
+      blocked[0] = blocked[1] = false;
+    }
+    if (filling) {
+      if (vol >= fillVol) break;
+      needIn = ri.frontier >= 0 && !blocked[0];
+      needOut = ro.frontier >= 0 && !blocked[1];
+      targetElems = std::max(ri.run, ro.run) * 2;
+    }
     if (!needIn && !needOut) break;
     int side = (needIn && (!needOut || ri.run <= ro.run)) ? 0 : 1;
     const RunInfo& rs = side == 0 ? ri : ro;
@@ -184,7 +198,7 @@ void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t*
     int64_t base = rs.run / e[fr];
     int64_t want = std::max(e[fr] + 1, ceilDiv(targetElems, base));
     int64_t enew = std::min<int64_t>(f.dim[fr], want);
-    int64_t cap = maxVol / (vol / e[fr]);
+    int64_t cap = (filling ? std::min(maxVol, fillVol * 2 - 1) : maxVol) / (vol / e[fr]);
     if (enew > cap) enew = cap;
     if (enew < f.dim[fr] && enew > e[fr]) enew = pickExtent(f.dim[fr], enew, e[fr], 16 / f.esize);
     if (enew <= e[fr]) {
@@ -306,23 +320,15 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide, const TileParams&
     }
     if (prefix % V != 0) return 1;
   }
-  // a ragged rank must be constant across a unit, or be the lowest tile
-  // rank with extent and dim multiples of V
-  for (int sl = 0; sl < tp.nRagged; ++sl) {
-    int t = tp.rgTR[sl];
-    int64_t stride = 1;
-    for (int i = 0; i < f.rank; ++i) {
-      int r = outputSide ? f.perm[i] : i;
-      if (trOfRank[r] == t) break;
-      stride *= e[r];
-    }
-    if (stride % V == 0) continue;
-    int r = -1;
-    for (int rr = 0; rr < f.rank; ++rr)
-      if (trOfRank[rr] == t) r = rr;
-    if (stride == 1 && e[r] % V == 0 && f.dim[r] % V == 0) continue;
-    return 1;
+  // a ragged rank's shifted last chunk starts at (dim - extent) * stride,
+  // which must stay a multiple of V
+  for (int r = 0; r < f.rank; ++r) {
+    if (f.dim[r] % e[r] == 0) continue;
+    int64_t s = outputSide ? f.sout[r] : f.sin[r];
+    if (((f.dim[r] - e[r]) * s) % V != 0) return 1;
   }
+  (void)tp;
+  (void)trOfRank;
   return V;
 }
 
@@ -361,7 +367,6 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
   // neighbouring output.
   int nGR = 0;
   int64_t numTiles = 1;
-  tp.rgTR[0] = tp.rgTR[1] = -1;
   for (int i = 0; i < f.rank; ++i) {
     int r = f.perm[i];
     int64_t nch = ceilDiv(f.dim[r], e[r]);
@@ -370,35 +375,15 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
     tp.grDiv[nGR] = makeFastDiv((uint32_t)nch);
     tp.grSin[nGR] = e[r] * f.sin[r];
     tp.grSout[nGR] = e[r] * f.sout[r];
-    tp.grRg[nGR] = -1;
-    if (f.dim[r] % e[r] != 0) {
-      if (tp.nRagged >= 2) return false;
-      int sl = tp.nRagged++;
-      tp.rgTR[sl] = trOfRank[r];
-      tp.rgDim[sl] = f.dim[r];
-      tp.rgE[sl] = (int)e[r];
-      tp.grRg[nGR] = sl;
-    }
+    tp.grLastIn[nGR] = (f.dim[r] - e[r]) * f.sin[r];
+    tp.grLastOut[nGR] = (f.dim[r] - e[r]) * f.sout[r];
+    if (f.dim[r] % e[r] != 0) ++tp.nRagged;
     numTiles *= nch;
     if (numTiles >= (int64_t(1) << 31)) return false;
     ++nGR;
   }
   tp.nGR = nGR;
   tp.numTiles = (uint32_t)numTiles;
-  int outStride[MAXR];
-  {
-    int so = 1;
-    for (int i = 0; i < nTR; ++i) {
-      outStride[tp.trOut[i]] = so;
-      so *= tp.trE[tp.trOut[i]];
-    }
-  }
-  for (int sl = 0; sl < 2; ++sl) {
-    int t = tp.rgTR[sl];
-    tp.rgEDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)tp.trE[t] : 1u);
-    tp.rgInDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)tp.trInTile[t] : 1u);
-    tp.rgOutDiv[sl] = makeFastDiv(t >= 0 ? (uint32_t)outStride[t] : 1u);
-  }
   // Units: requested widths, reduced to 1 where the layout does not allow.
   if (lv > 1 && unitFor(f, e, false, tp, trOfRank) < lv) lv = 1;
   if (sv > 1 && unitFor(f, e, true, tp, trOfRank) < sv) sv = 1;
@@ -425,8 +410,7 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
   int perVec = 16 / f.esize;
   if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
   if (tp.smStride + 16 > 65535) return false;  // shared indices are 16-bit
-  const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 +
-                         ((4 * (tp.nIn + tp.nOut) * (tp.nRagged > 0 ? 2 : 1) + 15) / 16) * 16;
+  const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
   smemBytes = tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
   return smemBytes <= 227 * 1024;
 }
@@ -511,22 +495,16 @@ int tileCtasPerSM(const PlanDesc& pd) {
   return std::max(1, std::min(std::min(bySmem, byRegs), 2048 / TILE_THREADS));
 }
 
-void decodeTileHost(const TileParams& tp, uint32_t tile, int64_t& bin, int64_t& bout,
-                    int& lim0, int& lim1) {
+void decodeTileHost(const TileParams& tp, uint32_t tile, int64_t& bin, int64_t& bout) {
   bin = bout = 0;
-  lim0 = lim1 = 1;
   uint32_t rem = tile;
   for (int g = 0; g < tp.nGR; ++g) {
     uint32_t q = fastDivHost(rem, tp.grDiv[g]);
     uint32_t c = rem - q * tp.grDiv[g].d;
     rem = q;
-    bin += (int64_t)c * tp.grSin[g];
-    bout += (int64_t)c * tp.grSout[g];
-    int sl = tp.grRg[g];
-    if (sl >= 0) {
-      int lim = (int)std::min<int64_t>(tp.rgE[sl], tp.rgDim[sl] - (int64_t)c * tp.rgE[sl]);
-      if (sl == 0) lim0 = lim; else lim1 = lim;
-    }
+    const bool last = c + 1 == tp.grDiv[g].d;
+    bin += last ? tp.grLastIn[g] : (int64_t)c * tp.grSin[g];
+    bout += last ? tp.grLastOut[g] : (int64_t)c * tp.grSout[g];
   }
 }
 
@@ -540,24 +518,19 @@ void modelTile(PlanDesc& pd, int numSMs) {
   for (int s = 0; s < samples; ++s) {
     uint32_t tile = (uint32_t)((int64_t)s * tp.numTiles / samples);
     int64_t bin, bout;
-    int lim0, lim1;
-    decodeTileHost(tp, tile, bin, bout, lim0, lim1);
+    decodeTileHost(tp, tile, bin, bout);
     si.clear();
     so.clear();
     std::unordered_map<int64_t, int> perSector;
     for (int j = 0; j < tp.tileVol; ++j) {
       int rem = j;
       int64_t oi = bin, oo = bout;
-      bool ok = true;
       for (int t = 0; t < tp.nTR; ++t) {
         int c = rem % tp.trE[t];
         rem /= tp.trE[t];
         oi += (int64_t)c * tp.trSin[t];
         oo += (int64_t)c * tp.trSout[t];
-        if (t == tp.rgTR[0] && c >= lim0) ok = false;
-        if (t == tp.rgTR[1] && c >= lim1) ok = false;
       }
-      if (!ok) continue;
       useful += 1;
       si.insert(oi * f.esize / 32);
       int64_t sec = oo * f.esize / 32;
@@ -657,14 +630,17 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
       }
     }
     // Tile candidates: (target contiguous run, maximum tile bytes).
-    const int knobs[][2] = {{512, 16384}, {256, 8192}, {128, 4096},  {1024, 32768},
-                            {512, 32768}, {256, 4096}, {2048, 65536}, {64, 2048}};
+    // (target contiguous run bytes, maximum tile bytes, minimum tile bytes)
+    const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
+                            {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
+                            {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
     std::vector<std::vector<int64_t>> seen;
     for (auto& kb : knobs) {
       int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
       int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
+      int64_t fillVol = std::min<int64_t>(maxVol, kb[2] / f.esize);
       int64_t e[MAXR];
-      chooseExtents(f, target, maxVol, e);
+      chooseExtents(f, target, maxVol, fillVol, e);
       std::vector<int64_t> key(e, e + f.rank);
       if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
       seen.push_back(key);

@@ -85,22 +85,21 @@ struct TileParams {
   int nGR;              // grid ranks (more than one chunk), decode order
   int padShift;         // smem index = j + ((j >> padShift) << padLog); PAD_NONE = none
   int smStride;         // elements per smem buffer including padding
-  int nRagged;          // ragged ranks (dim not a multiple of extent), <= 2
-  int rgTR[2];          // tile-rank index of each ragged rank
-  long long rgDim[2];   // its full dim
-  int rgE[2];           // its extent
-  FastDiv rgEDiv[2];    // division by the extent
-  FastDiv rgInDiv[2];   // by its in-tile input-order stride
-  FastDiv rgOutDiv[2];  // by its in-tile output-order stride
+  int nRagged;          // grid ranks whose dim is not a multiple of the extent
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
   int trSout[MAXR];     // global output stride of tile rank t (elements)
   int trOut[MAXR];      // tile ranks in output order (indices into tr*)
-  FastDiv grDiv[MAXR];  // number of chunks of grid rank g
-  int grRg[MAXR];       // ragged slot (0/1) of grid rank g, or -1
+  // Grid rank g has grDiv[g].d chunks; chunk c starts at c * extent, except
+  // that the last chunk starts at dim - extent, so that every tile is full
+  // (a ragged last chunk overlaps its neighbour; the overlap is written
+  // twice with identical bits).
+  FastDiv grDiv[MAXR];    // number of chunks of grid rank g
   long long grSin[MAXR];  // input step of one chunk of grid rank g
   long long grSout[MAXR]; // output step of one chunk of grid rank g
+  long long grLastIn[MAXR];   // input offset of the last chunk
+  long long grLastOut[MAXR];  // output offset of the last chunk
 };
 
 // Row-copy parameters (TiledCopy: input rank 0 is also output rank 0).

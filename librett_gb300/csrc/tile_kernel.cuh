@@ -11,11 +11,12 @@
 // Units never straddle a run boundary and are 16-byte aligned in global
 // memory; the planner only picks LV/SV > 1 when the layout guarantees this.
 //
-// Offsets of units relative to the tile base are the same for every tile, so
-// each CTA computes them once into shared-memory tables; only two 64-bit
-// bases change per tile.  Tiles cut by a ragged rank (dim not a multiple of
-// the extent) recover the coordinate along that rank with two invariant
-// divisions and skip units outside the tensor.
+// Every tile is full: along a rank whose dim is not a multiple of the
+// extent, the last chunk starts at dim - extent and overlaps its neighbour
+// (the overlap is loaded and stored twice with identical bits).  So no tile
+// needs bounds checks.  Offsets of units relative to the tile base are the
+// same for every tile; each CTA computes them once into shared-memory tables
+// and only two 64-bit bases change per tile.
 #pragma once
 
 #include "kernels.cuh"
@@ -23,46 +24,18 @@
 namespace lt {
 
 __device__ __forceinline__ void decodeTile(const TileParams& p, uint32_t tile, long long& bin,
-                                           long long& bout, unsigned& lim0, unsigned& lim1) {
+                                           long long& bout) {
   bin = 0;
   bout = 0;
-  lim0 = 0xffffu;
-  lim1 = 0xffffu;
   uint32_t rem = tile;
   for (int g = 0; g < p.nGR; ++g) {
     const uint32_t q = fdiv(rem, p.grDiv[g]);
     const uint32_t c = rem - q * p.grDiv[g].d;
     rem = q;
-    bin += (long long)c * p.grSin[g];
-    bout += (long long)c * p.grSout[g];
-    const int s = p.grRg[g];
-    if (s >= 0) {
-      // only the last chunk of a ragged rank is partial
-      const long long left = p.rgDim[s] - (long long)c * p.rgE[s];
-      if (left < p.rgE[s]) {
-        if (s == 0) lim0 = (unsigned)left; else lim1 = (unsigned)left;
-      }
-    }
+    const bool last = c + 1 == p.grDiv[g].d;
+    bin += last ? p.grLastIn[g] : (long long)c * p.grSin[g];
+    bout += last ? p.grLastOut[g] : (long long)c * p.grSout[g];
   }
-}
-
-// Coordinate along a ragged rank of in-tile index x, given the divisor of
-// that rank's in-tile stride (input or output order) and of its extent.
-__device__ __forceinline__ unsigned raggedCoord(uint32_t x, const FastDiv& strideDiv,
-                                                const FastDiv& extDiv) {
-  const uint32_t a = fdiv(x, strideDiv);
-  return a - fdiv(a, extDiv) * extDiv.d;
-}
-
-// A unit whose packed ragged coordinates are rg (coordinate along ragged
-// rank 0 in the low 16 bits, rank 1 in the high 16 bits) lies inside a tile
-// whose valid extents along those ranks are lim0 / lim1.
-__device__ __forceinline__ bool insideTile(unsigned rg, unsigned lim0, unsigned lim1) {
-  return (rg & 0xffffu) < lim0 && (rg >> 16) < lim1;
-}
-
-__device__ __forceinline__ bool fullTile(unsigned lim0, unsigned lim1) {
-  return (lim0 & lim1) == 0xffffu;
 }
 
 // Returns x unchanged, but the compiler cannot see through it: values derived
@@ -77,14 +50,8 @@ __device__ __forceinline__ int smemIndex(const TileParams& p, int j) {
   return j + ((j >> p.padShift) << p.padLog);
 }
 
-template <int BYTES>
-__device__ __forceinline__ void cpAsync(uint32_t dst, const void* src) {
-  if constexpr (BYTES == 16) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
-  } else {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES)
-                 : "memory");
-  }
+__device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
 }
 
 __device__ __forceinline__ void cpAsyncCommit() {
@@ -99,55 +66,40 @@ __device__ __forceinline__ void cpAsyncWait() {
 // Shared-memory tables, built once per CTA:
 //   ldOff[u]  global input offset (elements) of load unit u,
 //   stOff[w]  global output offset (elements) of store unit w,
-//   stSm[q]   shared-memory data index of output-order element q,
-//   rgIn[u], rgOut[w]  packed coordinates along the ragged ranks (only when
-//             the tile has ragged ranks).
+//   stSm[q]   shared-memory data index of output-order element q.
 struct TileTables {
   int* ldOff;
   int* stOff;
   unsigned short* stSm;
-  unsigned* rgIn;
-  unsigned* rgOut;
   unsigned char* data;  // data buffers follow the tables (16-byte aligned)
 };
 
-// Layout: stSm (2 bytes per element, padded to 16 bytes); ldOff, stOff and,
-// with ragged ranks, rgIn, rgOut (4 bytes per unit), padded to 16 bytes;
-// then the data buffers.
+// Layout: stSm (2 bytes per element, padded to 16 bytes); ldOff and stOff
+// (4 bytes per unit), padded to 16 bytes; then the data buffers.
 __host__ __device__ inline int tileSmIndexBytes(int vol) { return ((2 * vol + 15) / 16) * 16; }
 
-__host__ __device__ inline int tileTableBytes(int vol, int lv, int sv, int ragged) {
-  const int units = vol / lv + vol / sv;
-  return tileSmIndexBytes(vol) + ((4 * units * (ragged ? 2 : 1) + 15) / 16) * 16;
+__host__ __device__ inline int tileTableBytes(int vol, int lv, int sv) {
+  return tileSmIndexBytes(vol) + ((4 * (vol / lv + vol / sv) + 15) / 16) * 16;
 }
 
 __device__ __forceinline__ TileTables buildTileTables(const TileParams& p, unsigned char* smraw) {
   TileTables tt;
-  const bool ragged = p.nRagged > 0;
   tt.stSm = reinterpret_cast<unsigned short*>(smraw);
   tt.ldOff = reinterpret_cast<int*>(smraw + tileSmIndexBytes(p.tileVol));
   tt.stOff = tt.ldOff + p.nIn;
-  tt.rgIn = reinterpret_cast<unsigned*>(tt.stOff + p.nOut);
-  tt.rgOut = tt.rgIn + p.nIn;
-  tt.data = smraw + tileTableBytes(p.tileVol, p.lv, p.sv, ragged);
+  tt.data = smraw + tileTableBytes(p.tileVol, p.lv, p.sv);
   for (int u = threadIdx.x; u < p.nIn; u += blockDim.x) {
     int rem = u * p.lv, off = 0;
-    unsigned rg = 0;
     for (int t = 0; t < p.nTR; ++t) {
       const int e = p.trE[t];
       const int q = rem / e;
-      const int c = rem - q * e;
-      off += c * p.trSin[t];
+      off += (rem - q * e) * p.trSin[t];
       rem = q;
-      if (t == p.rgTR[0]) rg |= (unsigned)c;
-      if (t == p.rgTR[1]) rg |= (unsigned)c << 16;
     }
     tt.ldOff[u] = off;
-    if (ragged) tt.rgIn[u] = rg;
   }
   for (int q = threadIdx.x; q < p.tileVol; q += blockDim.x) {
     int rem = q, off = 0, jj = 0;
-    unsigned rg = 0;
     for (int i = 0; i < p.nTR; ++i) {
       const int t = p.trOut[i];
       const int e = p.trE[t];
@@ -156,14 +108,9 @@ __device__ __forceinline__ TileTables buildTileTables(const TileParams& p, unsig
       rem = d;
       off += c * p.trSout[t];
       jj += c * p.trInTile[t];
-      if (t == p.rgTR[0]) rg |= (unsigned)c;
-      if (t == p.rgTR[1]) rg |= (unsigned)c << 16;
     }
     tt.stSm[q] = (unsigned short)smemIndex(p, jj);
-    if (q % p.sv == 0) {
-      tt.stOff[q / p.sv] = off;
-      if (ragged) tt.rgOut[q / p.sv] = rg;
-    }
+    if (q % p.sv == 0) tt.stOff[q / p.sv] = off;
   }
   __syncthreads();
   return tt;
@@ -173,18 +120,17 @@ __device__ __forceinline__ TileTables buildTileTables(const TileParams& p, unsig
 // from shared memory and write them as one access.
 template <int ES, int SV>
 __device__ __forceinline__ void storeTile(const TileParams& p, const TileTables& tt,
-                                          const typename Word<ES>::T* s, void* outBase,
-                                          unsigned lim0, unsigned lim1) {
+                                          const typename Word<ES>::T* s,
+                                          typename Word<ES>::T* outBase) {
   using T = typename Word<ES>::T;
   using ST = typename Word<ES * SV>::T;
+  static_assert(sizeof(ST) == SV * sizeof(T), "unit size");
   const int tv = opaque(threadIdx.x);
-  const bool full = fullTile(lim0, lim1);
 #pragma unroll 4
   for (int w = tv; w < p.nOut; w += TILE_THREADS) {
-    if (!full && !insideTile(tt.rgOut[w], lim0, lim1)) continue;
-    const int off = tt.stOff[w];
+    T* dst = outBase + tt.stOff[w];
     if constexpr (SV == 1) {
-      *reinterpret_cast<T*>(reinterpret_cast<T*>(outBase) + off) = s[tt.stSm[w]];
+      *dst = s[tt.stSm[w]];
     } else {
       T e[SV];
       if constexpr (SV == 2) {
@@ -199,9 +145,8 @@ __device__ __forceinline__ void storeTile(const TileParams& p, const TileTables&
         e[3] = s[idx.y >> 16];
       }
       ST v;
-      static_assert(sizeof(ST) == SV * sizeof(T), "unit size");
       __builtin_memcpy(&v, e, sizeof(ST));
-      *reinterpret_cast<ST*>(reinterpret_cast<T*>(outBase) + off) = v;
+      *reinterpret_cast<ST*>(dst) = v;
     }
   }
 }
@@ -222,51 +167,43 @@ tileKernelReg(const __grid_constant__ TileParams p, const typename Word<ES>::T* 
   uint32_t tile = blockIdx.x;
   if (tile >= p.numTiles) return;
   long long bin, bout;
-  unsigned lim0, lim1;
-  decodeTile(p, tile, bin, bout, lim0, lim1);
+  decodeTile(p, tile, bin, bout);
 
   LT v[NL];
-  auto load = [&](long long base, unsigned l0, unsigned l1) {
+  auto load = [&](long long base) {
     const int tv = opaque(threadIdx.x);
-    const bool full = fullTile(l0, l1);
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int u = tv + k * TILE_THREADS;
-      if (u < p.nIn && (full || insideTile(tt.rgIn[u], l0, l1)))
-        v[k] = *reinterpret_cast<const LT*>(in + base + tt.ldOff[u]);
+      if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + base + tt.ldOff[u]);
     }
   };
-  load(bin, lim0, lim1);
+  load(bin);
 
   int buf = 0;
   for (;;) {
     T* s = sm + buf * p.smStride;
     {
       const int tv = opaque(threadIdx.x);
-      const bool full = fullTile(lim0, lim1);
 #pragma unroll
       for (int k = 0; k < NL; ++k) {
         const int u = tv + k * TILE_THREADS;
-        if (u < p.nIn && (full || insideTile(tt.rgIn[u], lim0, lim1)))
-          *reinterpret_cast<LT*>(s + smemIndex(p, u * LV)) = v[k];
+        if (u < p.nIn) *reinterpret_cast<LT*>(s + smemIndex(p, u * LV)) = v[k];
       }
     }
     __syncthreads();
     const uint32_t next = tile + gridDim.x;
     const bool more = next < p.numTiles;
     long long nbin = 0, nbout = 0;
-    unsigned nl0 = 0xffffu, nl1 = 0xffffu;
     if (more) {
-      decodeTile(p, next, nbin, nbout, nl0, nl1);
-      load(nbin, nl0, nl1);
+      decodeTile(p, next, nbin, nbout);
+      load(nbin);
     }
-    storeTile<ES, SV>(p, tt, s, out + bout, lim0, lim1);
+    storeTile<ES, SV>(p, tt, s, out + bout);
     if (!more) break;
     tile = next;
     bin = nbin;
     bout = nbout;
-    lim0 = nl0;
-    lim1 = nl1;
     buf ^= 1;
   }
 }
@@ -291,19 +228,14 @@ tileKernelAsync(const __grid_constant__ TileParams p, const typename Word<ES>::T
   const uint32_t nMine = (p.numTiles - first + G - 1) / G;
 
   auto issue = [&](uint32_t i) {
-    const uint32_t tile = first + i * G;
     long long bin, bout;
-    unsigned lim0, lim1;
-    decodeTile(p, tile, bin, bout, lim0, lim1);
+    decodeTile(p, first + i * G, bin, bout);
     const T* src = in + bin;
     const uint32_t dst = smBase + (uint32_t)((i % TILE_STAGES) * p.smStride) * ES;
     const int tv = opaque(threadIdx.x);
-    const bool full = fullTile(lim0, lim1);
 #pragma unroll 4
-    for (int u = tv; u < p.nIn; u += TILE_THREADS) {
-      if (full || insideTile(tt.rgIn[u], lim0, lim1))
-        cpAsync<16>(dst + (uint32_t)smemIndex(p, u * LV) * ES, src + tt.ldOff[u]);
-    }
+    for (int u = tv; u < p.nIn; u += TILE_THREADS)
+      cpAsync16(dst + (uint32_t)smemIndex(p, u * LV) * ES, src + tt.ldOff[u]);
   };
 
 #pragma unroll
@@ -319,9 +251,8 @@ tileKernelAsync(const __grid_constant__ TileParams p, const typename Word<ES>::T
     if (i + TILE_STAGES - 1 < nMine) issue(i + TILE_STAGES - 1);
     cpAsyncCommit();
     long long bin, bout;
-    unsigned lim0, lim1;
-    decodeTile(p, first + i * G, bin, bout, lim0, lim1);
-    storeTile<ES, SV>(p, tt, sm + (i % TILE_STAGES) * p.smStride, out + bout, lim0, lim1);
+    decodeTile(p, first + i * G, bin, bout);
+    storeTile<ES, SV>(p, tt, sm + (i % TILE_STAGES) * p.smStride, out + bout);
   }
   cpAsyncWait<0>();
 }

@@ -54,18 +54,27 @@ def _check_plan(dims, perm, es, candidate=-1):
     assert info["smem_bytes"] >= 2 * tvol * es
     ragged = sum(1 for d, e in zip(fd, ext) if d % e)
     assert ragged <= 2
-    # every element is covered by exactly one tile (small problems only)
+    # Every element is covered by a full tile; a ragged rank's last chunk
+    # starts at dim - extent, so chunks overlap by less than one chunk count
+    # along that rank (small problems only).
     if vol <= 1 << 16:
         sin = np.cumprod([1] + fd[:-1])
         seen = np.zeros(vol, dtype=np.int64)
         chunks = [range(-(-d // e)) for d, e in zip(fd, ext)]
         for c in itertools.product(*chunks):
-            lo = [ci * e for ci, e in zip(c, ext)]
-            hi = [min(l + e, d) for l, e, d in zip(lo, ext, fd)]
-            grids = np.meshgrid(*[np.arange(l, h) for l, h in zip(lo, hi)], indexing="ij")
+            lo = [min(ci * e, d - e) for ci, e, d in zip(c, ext, fd)]
+            grids = np.meshgrid(*[np.arange(l, l + e) for l, e in zip(lo, ext)], indexing="ij")
             idx = sum(g.astype(np.int64) * s for g, s in zip(grids, sin))
             np.add.at(seen, idx.reshape(-1), 1)
-        assert (seen == 1).all()
+        assert (seen >= 1).all()
+        tiles_total = int(np.prod([len(r) for r in chunks])) * tvol
+        assert seen.sum() == tiles_total
+        overlap = tiles_total / vol - 1.0
+        bound = 1.0
+        for d, e in zip(fd, ext):
+            nch = -(-d // e)
+            bound *= nch * e / d
+        assert overlap <= bound - 1.0 + 1e-9
     return info
 
 
