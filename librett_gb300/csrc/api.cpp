@@ -32,6 +32,15 @@ struct PlanObj {
   int device = 0;
   int numSMs = 0;
   int lastGrid = 0;
+  void* tablesAlloc = nullptr;  // device tables of flat-pipeline plans
+  lt::DeviceTables tables;
+  PlanObj() = default;
+  PlanObj(const PlanObj&) = delete;
+  PlanObj& operator=(const PlanObj&) = delete;
+  // Stream-ordered release: launches already enqueued on the plan's stream
+  // finish before the tables are freed (LibreTT's plan destructor calls
+  // cudaFree, which synchronises the device, src/plan.cpp:1696-1703).
+  ~PlanObj() { lt::destroyDeviceTables(tablesAlloc, stream); }
 };
 
 // Plans are held by shared_ptr so that an execute that has looked a plan up
@@ -106,6 +115,20 @@ void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   info->model_cost = pd.cost;
 }
 
+// Creates the plan object (device tables included) and stores it.
+librettResult activate(librettHandle* handle, const lt::PlanDesc& pd, cudaStream_t stream, int dev,
+                       int sms) {
+  auto obj = std::make_shared<PlanObj>();
+  obj->pd = pd;
+  obj->stream = stream;
+  obj->device = dev;
+  obj->numSMs = sms;
+  if (lt::createDeviceTables(pd, stream, &obj->tablesAlloc, &obj->tables) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
+  *handle = storePlan(std::move(obj));
+  return LIBRETT_SUCCESS;
+}
+
 // Shared by librettPlan and librett_c_plan_candidate: plan with the given
 // candidate (or the heuristic's choice when candidate < 0).
 librettResult planImpl(librettHandle* handle, int rank, const int* dim, const int* perm,
@@ -120,13 +143,7 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
-  auto obj = std::make_shared<PlanObj>();
-  obj->pd = cands[pick];
-  obj->stream = stream;
-  obj->device = dev;
-  obj->numSMs = sms;
-  *handle = storePlan(std::move(obj));
-  return LIBRETT_SUCCESS;
+  return activate(handle, cands[pick], stream, dev, sms);
 }
 
 }  // namespace
@@ -172,15 +189,22 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
   librettResult res = LIBRETT_SUCCESS;
   for (size_t c = 0; c < cands.size() && res == LIBRETT_SUCCESS; ++c) {
     int grid = 0;
+    void* alloc = nullptr;
+    lt::DeviceTables dt;
+    if (lt::createDeviceTables(cands[c], stream, &alloc, &dt) != cudaSuccess) {
+      res = LIBRETT_INTERNAL_ERROR;
+      break;
+    }
     if (cudaMemsetAsync(odata, 0xff, bytes, stream) != cudaSuccess ||
-        lt::launchPlan(cands[c], idata, odata, stream, sms, &grid) != cudaSuccess) {
+        lt::launchPlan(cands[c], &dt, idata, odata, stream, sms, &grid) != cudaSuccess) {
+      lt::destroyDeviceTables(alloc, stream);
       res = LIBRETT_INTERNAL_ERROR;
       break;
     }
     float candMs = -1.f;
     for (int rep = 0; rep < 3; ++rep) {
       if (cudaEventRecord(ev[0], stream) != cudaSuccess ||
-          lt::launchPlan(cands[c], idata, odata, stream, sms, &grid) != cudaSuccess ||
+          lt::launchPlan(cands[c], &dt, idata, odata, stream, sms, &grid) != cudaSuccess ||
           cudaEventRecord(ev[1], stream) != cudaSuccess || cudaEventSynchronize(ev[1]) != cudaSuccess) {
         res = LIBRETT_INTERNAL_ERROR;
         break;
@@ -189,6 +213,7 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
       cudaEventElapsedTime(&ms, ev[0], ev[1]);
       if (candMs < 0.f || ms < candMs) candMs = ms;
     }
+    lt::destroyDeviceTables(alloc, stream);
     if (res == LIBRETT_SUCCESS && (best < 0 || candMs < bestMs)) {
       best = (int)c;
       bestMs = candMs;
@@ -197,13 +222,7 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   if (res != LIBRETT_SUCCESS) return res;
-  auto obj = std::make_shared<PlanObj>();
-  obj->pd = cands[best];
-  obj->stream = stream;
-  obj->device = dev;
-  obj->numSMs = sms;
-  *handle = storePlan(std::move(obj));
-  return LIBRETT_SUCCESS;
+  return activate(handle, cands[best], stream, dev, sms);
 }
 
 librettResult librettDestroy(librettHandle handle) {
@@ -224,7 +243,8 @@ librettResult librettExecute(librettHandle handle, void* idata, void* odata) {
   if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   if (dev != obj->device) return LIBRETT_INVALID_DEVICE;
   int grid = 0;
-  if (lt::launchPlan(obj->pd, idata, odata, obj->stream, obj->numSMs, &grid) != cudaSuccess)
+  if (lt::launchPlan(obj->pd, &obj->tables, idata, odata, obj->stream, obj->numSMs, &grid) !=
+      cudaSuccess)
     return LIBRETT_INTERNAL_ERROR;
   obj->lastGrid = grid;
   return LIBRETT_SUCCESS;

@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -41,60 +42,84 @@ int cachedOccupancy(const void* func, int threads, int smem) {
 namespace {
 
 template <int US>
-cudaError_t launchCopy(const void* in, void* out, long long n, cudaStream_t s, int numSMs,
-                       int* grid) {
+cudaError_t launchCopy(const void* in, void* out, long long n, cudaStream_t s, int* grid) {
   using T = typename Word<US>::T;
-  auto fn = copyKernel<US>;
-  int occ = cachedOccupancy((const void*)fn, COPY_THREADS, 0);
-  if (occ < 1) return cudaErrorInvalidConfiguration;
-  long long want = (n + COPY_THREADS * 4 - 1) / (COPY_THREADS * 4);
-  long long g = std::min<long long>(want, (long long)numSMs * occ);
-  if (g < 1) g = 1;
+  const long long per = (long long)COPY_THREADS * COPY_UNROLL;
+  const long long g = (n + per - 1) / per;
+  if (g < 1 || g > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   *grid = (int)g;
-  fn<<<(unsigned)g, COPY_THREADS, 0, s>>>((const T*)in, (T*)out, n);
+  copyKernel<US><<<(unsigned)g, COPY_THREADS, 0, s>>>((const T*)in, (T*)out, n);
   return cudaGetLastError();
 }
 
 template <int US>
-cudaError_t launchRows(const RowParams& rp, const void* in, void* out, cudaStream_t s,
-                       int numSMs, int* grid) {
+cudaError_t launchRows(const RowParams& rp, const void* in, void* out, cudaStream_t s, int* grid) {
   using T = typename Word<US>::T;
-  auto fn = rowCopyKernel<US>;
-  int occ = cachedOccupancy((const void*)fn, ROW_THREADS, 0);
-  if (occ < 1) return cudaErrorInvalidConfiguration;
-  long long warpsPerCta = ROW_THREADS / 32;
-  long long want = ((long long)rp.numItems + warpsPerCta * 4 - 1) / (warpsPerCta * 4);
-  long long g = std::min<long long>(want, (long long)numSMs * occ);
-  if (g < 1) g = 1;
+  const long long g = ((long long)rp.numItems + ROW_ITEMS_PER_CTA - 1) / ROW_ITEMS_PER_CTA;
+  if (g < 1) return cudaErrorInvalidConfiguration;
   *grid = (int)g;
-  fn<<<(unsigned)g, ROW_THREADS, 0, s>>>(rp, (const T*)in, (T*)out);
+  rowCopyKernel<US><<<(unsigned)g, ROW_THREADS, 0, s>>>(rp, (const T*)in, (T*)out);
   return cudaGetLastError();
 }
 
 cudaError_t launchCopyUnit(int unit, const void* in, void* out, long long n, cudaStream_t s,
-                           int numSMs, int* grid) {
+                           int* grid) {
   switch (unit) {
-    case 4: return launchCopy<4>(in, out, n, s, numSMs, grid);
-    case 8: return launchCopy<8>(in, out, n, s, numSMs, grid);
-    case 16: return launchCopy<16>(in, out, n, s, numSMs, grid);
+    case 4: return launchCopy<4>(in, out, n, s, grid);
+    case 8: return launchCopy<8>(in, out, n, s, grid);
+    case 16: return launchCopy<16>(in, out, n, s, grid);
     default: return cudaErrorInvalidValue;
   }
 }
 
 cudaError_t launchRowsUnit(int unit, const RowParams& rp, const void* in, void* out,
-                           cudaStream_t s, int numSMs, int* grid) {
+                           cudaStream_t s, int* grid) {
   switch (unit) {
-    case 4: return launchRows<4>(rp, in, out, s, numSMs, grid);
-    case 8: return launchRows<8>(rp, in, out, s, numSMs, grid);
-    case 16: return launchRows<16>(rp, in, out, s, numSMs, grid);
+    case 4: return launchRows<4>(rp, in, out, s, grid);
+    case 8: return launchRows<8>(rp, in, out, s, grid);
+    case 16: return launchRows<16>(rp, in, out, s, grid);
     default: return cudaErrorInvalidValue;
   }
 }
 
 }  // namespace
 
-cudaError_t launchPlan(const PlanDesc& pd, const void* in, void* out, cudaStream_t s, int numSMs,
-                       int* grid) {
+cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt) {
+  *alloc = nullptr;
+  *dt = DeviceTables();
+  if (pd.kernel != K_TILE || pd.pipe != PIPE_FLAT) return cudaSuccess;
+  const TileParams& tp = pd.tile;
+  const size_t ldBytes = 4 * (size_t)tp.nIn, stBytes = 4 * (size_t)tp.nOut;
+  const size_t smBytes = 2 * (size_t)tp.tileVol;
+  const size_t total = ldBytes + stBytes + smBytes;
+  std::vector<unsigned char> host(total);
+  int* ld = reinterpret_cast<int*>(host.data());
+  int* st = reinterpret_cast<int*>(host.data() + ldBytes);
+  unsigned short* sm = reinterpret_cast<unsigned short*>(host.data() + ldBytes + stBytes);
+  tileTablesHost(tp, ld, st, sm);
+  void* d = nullptr;
+  cudaError_t err = cudaMallocAsync(&d, total, s);
+  if (err != cudaSuccess) return err;
+  // pageable source: the call returns once the bytes have been staged
+  err = cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s);
+  if (err != cudaSuccess) {
+    cudaFreeAsync(d, s);
+    return err;
+  }
+  *alloc = d;
+  unsigned char* b = static_cast<unsigned char*>(d);
+  dt->ldOff = reinterpret_cast<const int*>(b);
+  dt->stOff = reinterpret_cast<const int*>(b + ldBytes);
+  dt->stSm = reinterpret_cast<const unsigned short*>(b + ldBytes + stBytes);
+  return cudaSuccess;
+}
+
+void destroyDeviceTables(void* alloc, cudaStream_t s) {
+  if (alloc != nullptr) cudaFreeAsync(alloc, s);
+}
+
+cudaError_t launchPlan(const PlanDesc& pd, const DeviceTables* dt, const void* in, void* out,
+                       cudaStream_t s, int numSMs, int* grid) {
   const uintptr_t align = (uintptr_t)in | (uintptr_t)out;
   int g = 0;
   cudaError_t err = cudaErrorInvalidValue;
@@ -102,20 +127,21 @@ cudaError_t launchPlan(const PlanDesc& pd, const void* in, void* out, cudaStream
     case K_COPY: {
       int unit = (align % pd.unitBytes == 0) ? pd.unitBytes : pd.f.esize;
       long long n = pd.f.vol * pd.f.esize / unit;
-      err = launchCopyUnit(unit, in, out, n, s, numSMs, &g);
+      err = launchCopyUnit(unit, in, out, n, s, &g);
       break;
     }
     case K_ROW: {
       bool vec = align % pd.unitBytes == 0;
       err = launchRowsUnit(vec ? pd.unitBytes : pd.f.esize, vec ? pd.row : pd.rowScalar, in, out,
-                           s, numSMs, &g);
+                           s, &g);
       break;
     }
     case K_TILE: {
       const PlanDesc* use = &pd;
       PlanDesc scalar;
       if ((pd.tile.lv > 1 || pd.tile.sv > 1) && align % 16 != 0) {
-        // 16-byte units need 16-byte aligned tensors; fall back to elements
+        // 16-byte units need 16-byte aligned tensors; fall back to element
+        // units and the persistent pipeline, which builds its own tables
         scalar = pd;
         scalar.tile = pd.tileScalar;
         scalar.slots = pd.slotsScalar;
@@ -124,9 +150,9 @@ cudaError_t launchPlan(const PlanDesc& pd, const void* in, void* out, cudaStream
         use = &scalar;
       }
       switch (pd.f.esize) {
-        case 4: err = launchTile4(*use, in, out, s, numSMs, &g); break;
-        case 8: err = launchTile8(*use, in, out, s, numSMs, &g); break;
-        case 16: err = launchTile16(*use, in, out, s, numSMs, &g); break;
+        case 4: err = launchTile4(*use, dt, in, out, s, numSMs, &g); break;
+        case 8: err = launchTile8(*use, dt, in, out, s, numSMs, &g); break;
+        case 16: err = launchTile16(*use, dt, in, out, s, numSMs, &g); break;
         default: err = cudaErrorInvalidValue;
       }
       break;

@@ -8,11 +8,27 @@
 
 namespace lt {
 
+// Offset tables of a flat-pipeline tile plan, in device memory.
+struct DeviceTables {
+  const int* ldOff = nullptr;
+  const int* stOff = nullptr;
+  const unsigned short* stSm = nullptr;
+};
+
+// Builds the plan's tables on the host and uploads them into one
+// stream-ordered device allocation (cudaMallocAsync on s).  Plans of other
+// pipelines need none: *alloc = nullptr.
+cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt);
+
+// Releases them in stream order (cudaFreeAsync on s).
+void destroyDeviceTables(void* alloc, cudaStream_t s);
+
 // Launch whatever the plan describes on stream s.  Uses the 16-byte unit
 // variant when both pointers allow it, else the element-size one.  *grid
-// receives the number of CTAs launched.
-cudaError_t launchPlan(const PlanDesc& pd, const void* in, void* out, cudaStream_t s, int numSMs,
-                       int* grid);
+// receives the number of CTAs launched.  dt: the plan's device tables (flat
+// pipeline only).
+cudaError_t launchPlan(const PlanDesc& pd, const DeviceTables* dt, const void* in, void* out,
+                       cudaStream_t s, int numSMs, int* grid);
 
 // CTAs per SM of a kernel at a given dynamic smem size (cached per device);
 // raises the kernel's dynamic-smem limit when smem exceeds 48 KB.

@@ -218,6 +218,30 @@ void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t 
 
 }  // namespace
 
+void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short* stSm) {
+  for (int u = 0; u < tp.nIn; ++u) {
+    int rem = u * tp.lv, off = 0;
+    for (int t = 0; t < tp.nTR; ++t) {
+      const int c = rem % tp.trE[t];
+      rem /= tp.trE[t];
+      off += c * tp.trSin[t];
+    }
+    ldOff[u] = off;
+  }
+  for (int q = 0; q < tp.tileVol; ++q) {
+    int rem = q, off = 0, jj = 0;
+    for (int i = 0; i < tp.nTR; ++i) {
+      const int t = tp.trOut[i];
+      const int c = rem % tp.trE[t];
+      rem /= tp.trE[t];
+      off += c * tp.trSout[t];
+      jj += c * tp.trInTile[t];
+    }
+    stSm[q] = (unsigned short)(jj + ((jj >> tp.padShift) << tp.padLog));
+    if (q % tp.sv == 0) stOff[q / tp.sv] = off;
+  }
+}
+
 long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
   // Simulates one full tile: load-side unit writes and, for each element of
   // a store unit, the store-side element reads.  A phase of lanes covers 128
@@ -411,7 +435,10 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
   if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
   if (tp.smStride + 16 > 65535) return false;  // shared indices are 16-bit
   const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
-  smemBytes = tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
+  if (pipe == PIPE_FLAT)
+    smemBytes = tp.smStride * f.esize;  // one data buffer; tables live in device memory
+  else
+    smemBytes = tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
   return smemBytes <= 227 * 1024;
 }
 
@@ -549,6 +576,7 @@ void modelTile(PlanDesc& pd, int numSMs) {
   double conc = (double)numSMs * occ;
   double active = std::min<double>(conc, tp.numTiles);
   int ahead = pd.pipe == PIPE_ASYNC ? TILE_STAGES - 1 : 1;
+  if (pd.pipe == PIPE_FLAT) ahead = 1;
   double inflight = active * ahead * tp.tileVol * f.esize;  // loads in flight
   double tFlight = (double)f.vol * f.esize / std::max(1.0, inflight) * kLatency;
   double waves = std::ceil((double)tp.numTiles / conc);
@@ -644,7 +672,7 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
       std::vector<int64_t> key(e, e + f.rank);
       if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
       seen.push_back(key);
-      for (int pipe : {PIPE_REG, PIPE_ASYNC}) {
+      for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
         PlanDesc pd;
         pd.f = f;
         pd.pipe = pipe;

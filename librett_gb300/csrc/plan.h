@@ -25,7 +25,9 @@ constexpr int TILE_STAGES = 3;     // cp.async pipeline depth of the tile kernel
 
 // Tile pipelines: register-staged loads (2 shared buffers) or cp.async
 // straight into a TILE_STAGES-deep ring of shared buffers.
-enum Pipe { PIPE_REG = 0, PIPE_ASYNC = 1 };
+enum Pipe { PIPE_REG = 0, PIPE_ASYNC = 1, PIPE_FLAT = 2 };
+// PIPE_FLAT: one tile per CTA (no persistent loop); the offset tables are
+// built on the host at plan time and read from device memory.
 
 // Transpose methods, numbered as LibreTT's enum (src/plan.h:54-56).
 enum Method { Unknown = 0, Trivial = 1, Packed = 2, PackedSplit = 3, Tiled = 4, TiledCopy = 5 };
@@ -160,6 +162,10 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
 
 // Index of the candidate the analytic model prefers.
 int chooseHeuristic(const std::vector<PlanDesc>& cands);
+
+// Offset tables of a tile (the layout the tile kernels use, see
+// tile_kernel.cuh): ldOff[nIn], stOff[nOut], stSm[tileVol].
+void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short* stSm);
 
 // Shared-memory bank wavefronts of one full tile (load-side writes plus
 // store-side reads) for a given padding; exposed for tests.

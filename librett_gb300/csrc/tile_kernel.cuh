@@ -116,10 +116,12 @@ __device__ __forceinline__ TileTables buildTileTables(const TileParams& p, unsig
   return tt;
 }
 
-// Store phase shared by both pipelines: gather SV elements per store unit
-// from shared memory and write them as one access.
+// Store phase shared by all pipelines: gather SV elements per store unit
+// from shared memory and write them as one access.  stOff / stSm point to
+// the offset tables (shared memory or device memory).
 template <int ES, int SV>
-__device__ __forceinline__ void storeTile(const TileParams& p, const TileTables& tt,
+__device__ __forceinline__ void storeTile(const TileParams& p, const int* __restrict__ stOff,
+                                          const unsigned short* __restrict__ stSm,
                                           const typename Word<ES>::T* s,
                                           typename Word<ES>::T* outBase) {
   using T = typename Word<ES>::T;
@@ -128,17 +130,17 @@ __device__ __forceinline__ void storeTile(const TileParams& p, const TileTables&
   const int tv = opaque(threadIdx.x);
 #pragma unroll 4
   for (int w = tv; w < p.nOut; w += TILE_THREADS) {
-    T* dst = outBase + tt.stOff[w];
+    T* dst = outBase + stOff[w];
     if constexpr (SV == 1) {
-      *dst = s[tt.stSm[w]];
+      *dst = s[stSm[w]];
     } else {
       T e[SV];
       if constexpr (SV == 2) {
-        const unsigned idx = *reinterpret_cast<const unsigned*>(tt.stSm + 2 * w);
+        const unsigned idx = *reinterpret_cast<const unsigned*>(stSm + 2 * w);
         e[0] = s[idx & 0xffffu];
         e[1] = s[idx >> 16];
       } else {
-        const uint2 idx = *reinterpret_cast<const uint2*>(tt.stSm + 4 * w);
+        const uint2 idx = *reinterpret_cast<const uint2*>(stSm + 4 * w);
         e[0] = s[idx.x & 0xffffu];
         e[1] = s[idx.x >> 16];
         e[2] = s[idx.y & 0xffffu];
@@ -199,7 +201,7 @@ tileKernelReg(const __grid_constant__ TileParams p, const typename Word<ES>::T* 
       decodeTile(p, next, nbin, nbout);
       load(nbin);
     }
-    storeTile<ES, SV>(p, tt, s, out + bout);
+    storeTile<ES, SV>(p, tt.stOff, tt.stSm, s, out + bout);
     if (!more) break;
     tile = next;
     bin = nbin;
@@ -252,9 +254,39 @@ tileKernelAsync(const __grid_constant__ TileParams p, const typename Word<ES>::T
     cpAsyncCommit();
     long long bin, bout;
     decodeTile(p, first + i * G, bin, bout);
-    storeTile<ES, SV>(p, tt, sm + (i % TILE_STAGES) * p.smStride, out + bout);
+    storeTile<ES, SV>(p, tt.stOff, tt.stSm, sm + (i % TILE_STAGES) * p.smStride, out + bout);
   }
   cpAsyncWait<0>();
+}
+
+// Flat pipeline: one tile per CTA and no persistent loop, so the hardware
+// block scheduler streams tiles through the SMs in order.  The offset tables
+// were built on the host at plan time and are read from device memory
+// (L1/L2-resident: every CTA of the launch reads the same few kilobytes).
+template <int ES, int LV, int SV, int NL>
+__global__ void __launch_bounds__(TILE_THREADS)
+tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T* __restrict__ in,
+               typename Word<ES>::T* __restrict__ out, const int* __restrict__ ldOff,
+               const int* __restrict__ stOff, const unsigned short* __restrict__ stSm) {
+  using T = typename Word<ES>::T;
+  using LT = typename Word<ES * LV>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* s = reinterpret_cast<T*>(smraw);
+  long long bin, bout;
+  decodeTile(p, blockIdx.x, bin, bout);
+  LT v[NL];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    const int u = threadIdx.x + k * TILE_THREADS;
+    if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + __ldg(ldOff + u));
+  }
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    const int u = threadIdx.x + k * TILE_THREADS;
+    if (u < p.nIn) *reinterpret_cast<LT*>(s + smemIndex(p, u * LV)) = v[k];
+  }
+  __syncthreads();
+  storeTile<ES, SV>(p, stOff, stSm, s, out + bout);
 }
 
 }  // namespace lt
