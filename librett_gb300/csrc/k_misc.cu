@@ -89,7 +89,10 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
   *dt = DeviceTables();
   if (pd.kernel != K_TILE || pd.pipe != PIPE_FLAT) return cudaSuccess;
   const TileParams& tp = pd.tile;
-  const size_t ldBytes = 4 * (size_t)tp.nIn, stBytes = 4 * (size_t)tp.nOut;
+  const size_t ldBytes = 4 * (size_t)tp.nIn;
+  // stSm is read 4 or 8 bytes at a time by the store gathers: keep it
+  // 16-byte aligned
+  const size_t stBytes = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16 - ldBytes;
   const size_t smBytes = 2 * (size_t)tp.tileVol;
   const size_t total = ldBytes + stBytes + smBytes;
   std::vector<unsigned char> host(total);

@@ -116,7 +116,9 @@ def test_every_candidate(cuda):
     rng = np.random.default_rng(7)
     probs = [([64, 48, 32], [2, 0, 1], 4), ([4, 6, 128, 5, 16], [3, 0, 4, 2, 1], 16),
              ([2, 3, 4, 5, 512, 16], [5, 3, 1, 4, 0, 2], 4), ([300, 7, 11], [0, 2, 1], 8),
-             ([33, 65, 17], [1, 2, 0], 8), ([1024, 1024], [1, 0], 4)]
+             ([33, 65, 17], [1, 2, 0], 8), ([1024, 1024], [1, 0], 4),
+             # element loads with 16-byte stores and an odd unit count
+             ([51, 2, 1354, 2, 9], [1, 3, 0, 2, 4], 4)]
     for dims, perm, es in probs:
         n = L.describe(dims, perm, es)["num_candidates"]
         assert n >= 1
