@@ -93,6 +93,24 @@ int librett_c_plan_candidate(librettHandle* handle, int rank, const int* dim,
                              const int* permutation, size_t sizeofType, void* stream,
                              int candidate);
 
+/* Transpose in one call without allocating device memory; no counterpart in
+ * LibreTT.  For callers that may not allocate device memory while running
+ * (device memory reserved up front by their own allocator, or allocation
+ * forbidden on a latency-critical path); librett_c_plan may allocate the
+ * offset tables of its plan, this call does not.  It plans on the host,
+ * writes the tile's offset tables into one fixed 64 KiB device array that
+ * the library holds on every GPU that loads it, and launches on `stream`.
+ * Returns LIBRETT_INVALID_PARAMETER if a tile's tables would exceed the
+ * array (cannot happen for tiles this planner makes).  The first call on a
+ * device looks up the array's address on that device: make it before any
+ * stream capture.  All calls share the array and every call rewrites the
+ * part it reads, so nothing needs to start at zero; calls that can overlap
+ * on the GPU (other streams, other host threads) race on it and must be
+ * ordered by the caller.  Inputs and outputs as for librett_c_execute. */
+int librett_c_transpose_noalloc(int rank, const int* dim, const int* permutation,
+                                size_t sizeofType, void* stream, const void* idata,
+                                void* odata);
+
 /* Number of device kernel launches this library issued since load (all
  * threads, all devices).  Used to count launches inside a timed region. */
 unsigned long long librett_c_launch_count(void);

@@ -114,6 +114,15 @@ def describe(dim, permutation, sizeofType: int, num_sms: int = 152,
     return info.as_dict()
 
 
+def transpose_noalloc(dim, permutation, sizeofType: int, stream, idata: int, odata: int) -> int:
+    """One-shot transpose that allocates no device memory
+    (librett_c_transpose_noalloc; no LibreTT counterpart).  Returns the
+    librettResult code."""
+    return _lib.load().librett_c_transpose_noalloc(len(dim), _lib.int_array(dim),
+                                                   _lib.int_array(permutation), sizeofType,
+                                                   _stream(stream), idata, odata)
+
+
 def launch_count() -> int:
     return int(_lib.load().librett_c_launch_count())
 

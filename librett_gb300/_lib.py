@@ -88,6 +88,8 @@ C_FUNCTIONS = [
       ctypes.POINTER(PlanInfo)]),
     ("librett_c_plan_candidate", ctypes.c_int,
      [ctypes.POINTER(_H), ctypes.c_int, _IP, _IP, ctypes.c_size_t, _P, ctypes.c_int]),
+    ("librett_c_transpose_noalloc", ctypes.c_int,
+     [ctypes.c_int, _IP, _IP, ctypes.c_size_t, _P, _P, _P]),
     ("librett_c_launch_count", ctypes.c_ulonglong, []),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]

@@ -1,0 +1,66 @@
+"""The no-allocation entry point against the regular plan/execute path.
+
+librett_c_transpose_noalloc serves callers that may not allocate device
+memory while running (all device memory reserved up front by their own
+allocator, or allocation forbidden on a latency-critical path).  It keeps
+the flat tile kernel's offset tables in one fixed device array instead of a
+per-plan allocation.  Here its outputs must equal, bit for bit, the outputs
+of librettPlan + librettExecute on the same inputs, on two calls in a row
+(the second call reuses the array the first one wrote).  The file sorts
+last so that a run stopping at the first failure has run everything else.
+"""
+import numpy as np
+import pytest
+
+import librett_gb300 as L
+from oracle import oracle as O
+from tests import shapes as S
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    S.C1,
+    ([4, 6, 64, 5, 32], [3, 0, 4, 2, 1], 16),
+    ([2, 3, 4, 5, 512, 16], [5, 3, 1, 4, 0, 2], 4),
+    ([51, 2, 1354, 2, 9], [1, 3, 0, 2, 4], 4),
+    ([201, 91, 63, 17], [2, 1, 3, 0], 8),
+    ([1000, 3, 7], [0, 2, 1], 8),      # leading rank shared
+    ([3, 4, 5], [0, 1, 2], 16),        # plain copy
+    (S.EXAMPLE[0], S.EXAMPLE[1], 8),
+]
+
+
+@pytest.mark.parametrize("dims,perm,es", CASES)
+def test_noalloc_matches_plan_execute(cuda, dims, perm, es):
+    import torch
+
+    rng = np.random.default_rng(sum(dims) + es)
+    vol = int(np.prod(dims))
+    host = rng.integers(0, 256, vol * es, dtype=np.uint8)
+    inp = torch.from_numpy(host).cuda()
+    ref = torch.zeros_like(inp)
+    stream = torch.cuda.current_stream()
+    with L.Plan(dims, perm, es, stream) as plan:
+        plan.execute(inp.data_ptr(), ref.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(ref.cpu().numpy(), O.transpose_np(host, dims, perm, es).view(np.uint8))
+    for call in range(2):
+        out = torch.full_like(inp, 0x5A)
+        rc = L.transpose_noalloc(dims, perm, es, stream, inp.data_ptr(), out.data_ptr())
+        assert rc == L.LIBRETT_SUCCESS, (call, rc)
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref), (dims, perm, es, call)
+
+
+def test_noalloc_rejects_bad_arguments(cuda):
+    import torch
+
+    buf = torch.zeros(1024, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(1024, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    assert L.transpose_noalloc([16, 16], [1, 0], 4, s, buf.data_ptr(),
+                               buf.data_ptr()) == L.LIBRETT_INVALID_PARAMETER
+    assert L.transpose_noalloc([16, 16], [1, 1], 4, s, buf.data_ptr(),
+                               out.data_ptr()) == L.LIBRETT_INVALID_PARAMETER
+    assert L.transpose_noalloc([16, 16], [1, 0], 4, s, buf.data_ptr() + 2,
+                               out.data_ptr()) == L.LIBRETT_INVALID_PARAMETER
