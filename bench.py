@@ -334,6 +334,13 @@ def run_engine(args):
         pk["launches"] += args.steps
         pk["ms"] += sum(ts)
         pk["bytes"] += 2 * problem_bytes(problems[k]) * args.steps
+    if args.per_problem:
+        with open(args.per_problem, "w") as fpp:
+            for (dims, perm, es), t, info in zip(problems, per_problem_ms, infos):
+                fpp.write(json.dumps({"dims": dims, "perm": perm, "es": es, "ms": t,
+                                      "gbs": 2 * problem_bytes((dims, perm, es)) / (t / 1e3) / 1e9,
+                                      "method": info["method"], "pipeline": info["pipeline"],
+                                      "tile": info["tile_extent"]}) + "\n")
     dom = max(per_kernel, key=lambda n: per_kernel[n]["ms"])
     d = per_kernel[dom]
     peak, peak_kind = load_peaks()
@@ -440,6 +447,8 @@ def main(argv=None):
     ap.add_argument("--dims", type=str, default=None, help="custom problem: comma-separated dims")
     ap.add_argument("--perm", type=str, default=None, help="custom problem: permutation")
     ap.add_argument("--es", type=int, default=8, help="custom problem: element bytes")
+    ap.add_argument("--per-problem", type=str, default=None,
+                    help="write one JSON line per problem (median launch time) to this file")
     ap.add_argument("--candidate", type=int, default=None,
                     help="plan every problem with this planner candidate (default: heuristic)")
     args = ap.parse_args(argv)

@@ -1,0 +1,115 @@
+"""Build and run LibreTT's own CUDA build -- TEST INFRASTRUCTURE ONLY.
+
+Compiles LibreTT's library sources, unmodified, from a source directory
+(default: the LibreTT checkout's src/) together with ref_driver.cpp into
+oracle/_ref/ref_driver with nvcc for sm_103a, then:
+
+  --golden : runs every case of tests/golden/golden.json through LibreTT's
+             librettPlan + librettExecute and compares the sha256 of each
+             output with the fixture (pins the fixtures to LibreTT itself);
+  --bench  : times LibreTT on the small case, the two small-leading-dimension
+             cases and the first --suite problems of the random-shape suite.
+
+Usage: python oracle/ref_bench/run_ref.py --src <LibreTT src dir> --out <dir>
+       [--golden] [--bench] [--suite N] [--measure]
+Writes JSON results under --out.  Nothing here is used by the engine.
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+REF = ROOT / "oracle" / "_ref"
+DRIVER = REF / "ref_driver"
+LIB_SOURCES = ["librett.cpp", "plan.cpp", "kernel.cpp", "GpuModel.cpp", "GpuModelKernel.cpp",
+               "GpuUtils.cpp", "Timer.cpp"]
+
+
+def build(src: Path) -> Path:
+    REF.mkdir(parents=True, exist_ok=True)
+    nvcc = os.environ.get("NVCC", "nvcc")
+    cmd = [nvcc, "-O3", "-std=c++17", "-DLIBRETT_USES_CUDA", "-gencode",
+           "arch=compute_103a,code=sm_103a", "-w", f"-I{src}", "-x", "cu",
+           *[str(src / f) for f in LIB_SOURCES], str(HERE / "ref_driver.cpp"), "-o", str(DRIVER)]
+    subprocess.run(cmd, check=True)
+    return DRIVER
+
+
+def write_cases(path: Path, cases):
+    kinds = {"value": 0, "words": 1, "none": 2}
+    with open(path, "w") as f:
+        for dims, perm, es, kind in cases:
+            f.write(" ".join(map(str, [len(dims), *dims, *perm, es, kinds[kind]])) + "\n")
+
+
+def run_golden(out: Path) -> dict:
+    rows = json.loads((ROOT / "tests" / "golden" / "golden.json").read_text())
+    cases = [(r["dims"], r["perm"], r["es"], r["input"]) for r in rows]
+    cf = out / "golden_cases.txt"
+    write_cases(cf, cases)
+    od = Path("/tmp/librett_ref_golden")
+    od.mkdir(parents=True, exist_ok=True)
+    subprocess.run([str(DRIVER), "golden", str(cf), str(od)], check=True)
+    result = []
+    for n, r in enumerate(rows):
+        data = (od / f"out_{n}.bin").read_bytes()
+        h = hashlib.sha256(data).hexdigest()
+        result.append({"dims": r["dims"], "perm": r["perm"], "es": r["es"], "input": r["input"],
+                       "match": h == r["sha256"], "reference_sha256": h})
+        (od / f"out_{n}.bin").unlink()
+    summary = {"cases": len(result), "matching": sum(x["match"] for x in result),
+               "rows": result}
+    (out / "reference_golden.json").write_text(json.dumps(summary, indent=1) + "\n")
+    return summary
+
+
+def run_bench(out: Path, nsuite: int, measure: bool, steps: int = 10, warmup: int = 3):
+    sys.path.insert(0, str(ROOT))
+    import bench as B
+
+    cases = [(d, p, es, "none") for d, p, es in
+             (B.workload_problems("c1", 1) + B.workload_problems("c3a", 1) +
+              B.workload_problems("c3b", 1) + B.suite_problems(200)[:nsuite])]
+    cf = out / "bench_cases.txt"
+    write_cases(cf, cases)
+    res = subprocess.run([str(DRIVER), "bench", str(cf), str(steps), str(warmup),
+                          "1" if measure else "0"], check=True, capture_output=True, text=True)
+    lines = [json.loads(x) for x in res.stdout.splitlines() if x.startswith("{")]
+    name = "reference_bench_measure.jsonl" if measure else "reference_bench.jsonl"
+    (out / name).write_text("".join(json.dumps(x) + "\n" for x in lines))
+    return lines
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--src", default="/root/reference/src")
+    ap.add_argument("--out", default=str(ROOT / "gpurun_out" / "ref"))
+    ap.add_argument("--golden", action="store_true")
+    ap.add_argument("--bench", action="store_true")
+    ap.add_argument("--measure", action="store_true", help="bench with librettPlanMeasure")
+    ap.add_argument("--suite", type=int, default=40)
+    args = ap.parse_args(argv)
+    out = Path(args.out)
+    out.mkdir(parents=True, exist_ok=True)
+    build(Path(args.src))
+    if args.golden:
+        s = run_golden(out)
+        print(f"golden: {s['matching']}/{s['cases']} outputs of LibreTT match the fixtures")
+    if args.bench:
+        lines = run_bench(out, args.suite, False)
+        print(f"bench: {len(lines)} cases timed")
+        if args.measure:
+            lines = run_bench(out, args.suite, True)
+            print(f"bench (plan measure): {len(lines)} cases timed")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
