@@ -143,6 +143,7 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  if (!lt::finalizePlan(cands[pick])) return LIBRETT_INTERNAL_ERROR;
   return activate(handle, cands[pick], stream, dev, sms);
 }
 
@@ -191,7 +192,8 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
     int grid = 0;
     void* alloc = nullptr;
     lt::DeviceTables dt;
-    if (lt::createDeviceTables(cands[c], stream, &alloc, &dt) != cudaSuccess) {
+    if (!lt::finalizePlan(cands[c]) ||
+        lt::createDeviceTables(cands[c], stream, &alloc, &dt) != cudaSuccess) {
       res = LIBRETT_INTERNAL_ERROR;
       break;
     }

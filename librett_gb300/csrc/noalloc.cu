@@ -132,6 +132,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
         flat = (int)c;
     if (flat >= 0) pick = flat;
   }
+  if (!finalizePlan(cands[pick])) return LIBRETT_INTERNAL_ERROR;
   const PlanDesc& pd = cands[pick];
   DeviceTables dt;
   const bool vecOk = ((uintptr_t)idata % 16 == 0 && (uintptr_t)odata % 16 == 0) ||

@@ -242,16 +242,14 @@ void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short
   }
 }
 
-long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
-  // Simulates one full tile: load-side unit writes and, for each element of
-  // a store unit, the store-side element reads.  A phase of lanes covers 128
-  // bytes; its wavefronts are the largest number of distinct 4-byte words
-  // any bank is asked for.
+long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits) {
+  // Simulates the first sampleUnits load units (one per lane) and store
+  // units (one instruction per element of a unit) of a tile.  A phase of
+  // lanes covers 128 bytes; its wavefronts are the largest number of
+  // distinct 4-byte words any bank is asked for.
   const int words = esize / 4;
   auto smIdx = [&](int j) { return j + ((j >> padShift) << tp.padLog); };
-  long long total = 0;
-  std::vector<int> jOfQ(tp.tileVol);
-  for (int q = 0; q < tp.tileVol; ++q) {
+  auto jOfQ = [&](int q) {
     int rem = q, jj = 0;
     for (int i = 0; i < tp.nTR; ++i) {
       int t = tp.trOut[i];
@@ -259,27 +257,27 @@ long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
       rem /= tp.trE[t];
       jj += c * tp.trInTile[t];
     }
-    jOfQ[q] = jj;
-  }
-  auto phaseCost = [&](const int* addr, const bool* act, int lanes, int wordsPerLane) {
+    return jj;
+  };
+  auto phaseCost = [&](const int* addr, const bool* act, int wordsPerLane) {
     long long cost = 0;
-    int lanesPerPhase = std::max(1, 32 / wordsPerLane);
-    for (int ph = 0; ph < lanes; ph += lanesPerPhase) {
+    const int lanesPerPhase = std::max(1, 32 / wordsPerLane);
+    for (int ph = 0; ph < 32; ph += lanesPerPhase) {
+      // per bank: distinct words (each lane touches wordsPerLane consecutive
+      // words, so one lane never hits a bank twice)
+      int words_[32][4];
       int cnt[32] = {};
       int maxPerBank = 0;
-      int seen[32 * 4];
-      int nSeen = 0;
-      for (int l = ph; l < std::min(lanes, ph + lanesPerPhase); ++l) {
+      for (int l = ph; l < ph + lanesPerPhase; ++l) {
         if (!act[l]) continue;
         for (int q = 0; q < wordsPerLane; ++q) {
-          int wa = addr[l] + q;
+          const int wa = addr[l] + q, bk = wa & 31;
           bool dup = false;
-          for (int s2 = 0; s2 < nSeen; ++s2)
-            if (seen[s2] == wa) { dup = true; break; }
+          for (int k = 0; k < cnt[bk] && k < 4; ++k)
+            if (words_[bk][k] == wa) { dup = true; break; }
           if (dup) continue;
-          seen[nSeen++] = wa;
-          int b = wa & 31;
-          if (++cnt[b] > maxPerBank) maxPerBank = cnt[b];
+          if (cnt[bk] < 4) words_[bk][cnt[bk]] = wa;
+          if (++cnt[bk] > maxPerBank) maxPerBank = cnt[bk];
         }
       }
       cost += maxPerBank;
@@ -288,24 +286,24 @@ long long smemWavefronts(const TileParams& tp, int esize, int padShift) {
   };
   int addr[32];
   bool act[32];
-  // load side: one unit of lv elements per lane
-  for (int base = 0; base < tp.nIn; base += 32) {
+  long long total = 0;
+  const int nIn = std::min(tp.nIn, sampleUnits), nOut = std::min(tp.nOut, sampleUnits);
+  for (int base = 0; base < nIn; base += 32) {
     for (int l = 0; l < 32; ++l) {
       int u = base + l;
-      act[l] = u < tp.nIn;
+      act[l] = u < nIn;
       addr[l] = act[l] ? smIdx(u * tp.lv) * words : 0;
     }
-    total += phaseCost(addr, act, 32, words * tp.lv);
+    total += phaseCost(addr, act, words * tp.lv);
   }
-  // store side: element m of each lane's store unit, one instruction per m
-  for (int base = 0; base < tp.nOut; base += 32) {
+  for (int base = 0; base < nOut; base += 32) {
     for (int m = 0; m < tp.sv; ++m) {
       for (int l = 0; l < 32; ++l) {
         int w = base + l;
-        act[l] = w < tp.nOut;
-        addr[l] = act[l] ? smIdx(jOfQ[w * tp.sv + m]) * words : 0;
+        act[l] = w < nOut;
+        addr[l] = act[l] ? smIdx(jOfQ(w * tp.sv + m)) * words : 0;
       }
-      total += phaseCost(addr, act, 32, words);
+      total += phaseCost(addr, act, words);
     }
   }
   return total;
@@ -325,16 +323,14 @@ int log2i(int x) {
   return l;
 }
 
-// Largest unit (elements) that never straddles a run boundary or a partial
-// tile edge and stays 16-byte aligned, for one side (input or output order).
-int unitFor(const Fused& f, const int64_t* e, bool outputSide, const TileParams& tp,
-            const int* trOfRank) {
+// Largest unit (elements) that never straddles a run boundary and stays
+// 16-byte aligned for one side (input or output order), including the
+// shifted last chunks of ragged ranks.
+int unitFor(const Fused& f, const int64_t* e, bool outputSide) {
   const int V = 16 / f.esize;
   if (V == 1) return 1;
   RunInfo ri = runOf(f, e, outputSide);
   if (ri.run % V != 0) return 1;
-  // dims of the ranks up to the frontier (in that order) must make every
-  // stride beyond the run a multiple of V
   if (ri.frontier >= 0) {
     int64_t prefix = 1;
     for (int i = 0; i < f.rank; ++i) {
@@ -344,22 +340,20 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide, const TileParams&
     }
     if (prefix % V != 0) return 1;
   }
-  // a ragged rank's shifted last chunk starts at (dim - extent) * stride,
-  // which must stay a multiple of V
   for (int r = 0; r < f.rank; ++r) {
     if (f.dim[r] % e[r] == 0) continue;
     int64_t s = outputSide ? f.sout[r] : f.sin[r];
     if (((f.dim[r] - e[r]) * s) % V != 0) return 1;
   }
-  (void)tp;
-  (void)trOfRank;
   return V;
 }
 
-// Fills tp for extents e with the given units; returns false when the tile
-// does not fit the kernel's limits.
-bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe, TileParams& tp,
-                     int& smemBytes) {
+// Tile geometry for extents e with the requested units (reduced to element
+// units where the layout does not allow them): tile and grid ranks, units,
+// and the padding that minimises shared-memory bank wavefronts.  Shared by
+// the three pipelines.  Returns false when the tile does not fit the
+// kernels' limits.
+bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
@@ -408,22 +402,19 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
   }
   tp.nGR = nGR;
   tp.numTiles = (uint32_t)numTiles;
-  // Units: requested widths, reduced to 1 where the layout does not allow.
-  if (lv > 1 && unitFor(f, e, false, tp, trOfRank) < lv) lv = 1;
-  if (sv > 1 && unitFor(f, e, true, tp, trOfRank) < sv) sv = 1;
-  if (pipe == PIPE_ASYNC && lv * f.esize != 16) return false;
+  if (lv > 1 && unitFor(f, e, false) < lv) lv = 1;
+  if (sv > 1 && unitFor(f, e, true) < sv) sv = 1;
   tp.lv = lv;
   tp.sv = sv;
   tp.padLog = log2i(lv);
   tp.nIn = tp.tileVol / lv;
   tp.nOut = tp.tileVol / sv;
-  // Padding that minimises shared-memory bank wavefronts.
   long long best = -1;
   int bestShift = PAD_NONE;
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
     if (sh < tp.padLog) continue;
-    long long w = smemWavefronts(tp, f.esize, sh);
+    long long w = smemWavefronts(tp, f.esize, sh, 64);
     if (best < 0 || w < best) {
       best = w;
       bestShift = sh;
@@ -434,33 +425,33 @@ bool buildTileParams(const Fused& f, const int64_t* e, int lv, int sv, int pipe,
   int perVec = 16 / f.esize;
   if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
   if (tp.smStride + 16 > 65535) return false;  // shared indices are 16-bit
-  const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
-  if (pipe == PIPE_FLAT)
-    smemBytes = tp.smStride * f.esize;  // one data buffer; tables live in device memory
-  else
-    smemBytes = tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * f.esize;
-  return smemBytes <= 227 * 1024;
+  return true;
 }
 
-bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
-  const int V = 16 / f.esize;
-  int smem = 0, smemScalar = 0;
-  if (!buildTileParams(f, e, V, V, pd.pipe, pd.tile, smem)) return false;
-  // misaligned pointers fall back to element-size units
-  if (!buildTileParams(f, e, 1, 1, PIPE_REG, pd.tileScalar, smemScalar)) return false;
-  const TileParams& tp = pd.tile;
+// Dynamic shared memory of a tile plan for one pipeline.
+int tileSmemBytes(const TileParams& tp, int esize, int pipe) {
+  if (pipe == PIPE_FLAT) return tp.smStride * esize;  // tables live in device memory
+  const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
+  return tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * esize;
+}
+
+// PlanDesc of a tile candidate from its geometry and pipeline.
+bool buildTile(const Fused& f, const int64_t* e, int pipe, const TileParams& geom, PlanDesc& pd) {
+  if (pipe == PIPE_ASYNC && geom.lv * f.esize != 16) return false;
+  const int smem = tileSmemBytes(geom, f.esize, pipe);
+  if (smem > 227 * 1024) return false;
+  pd.pipe = pipe;
+  pd.tile = geom;
   for (int r = 0; r < f.rank; ++r) pd.extent[r] = e[r];
   pd.kernel = K_TILE;
   pd.threads = TILE_THREADS;
-  pd.slots = nextPow2((tp.nIn + TILE_THREADS - 1) / TILE_THREADS);
-  pd.slotsScalar = nextPow2((pd.tileScalar.nIn + TILE_THREADS - 1) / TILE_THREADS);
-  pd.ragged = tp.nRagged > 0;
+  pd.slots = nextPow2((geom.nIn + TILE_THREADS - 1) / TILE_THREADS);
+  pd.ragged = geom.nRagged > 0;
   pd.smemBytes = smem;
-  pd.smemBytesScalar = smemScalar;
-  pd.padShift = tp.padShift;
-  pd.unitBytes = tp.lv * f.esize;
-  pd.unitOutBytes = tp.sv * f.esize;
-  pd.numWork = tp.numTiles;
+  pd.padShift = geom.padShift;
+  pd.unitBytes = geom.lv * f.esize;
+  pd.unitOutBytes = geom.sv * f.esize;
+  pd.numWork = geom.numTiles;
   RunInfo ri = runOf(f, e, false), ro = runOf(f, e, true);
   pd.runInBytes = (int)std::min<int64_t>(ri.run * f.esize, 1 << 30);
   pd.runOutBytes = (int)std::min<int64_t>(ro.run * f.esize, 1 << 30);
@@ -469,7 +460,7 @@ bool buildTile(const Fused& f, const int64_t* e, PlanDesc& pd) {
   bool partial = false;
   for (int r = 0; r < f.rank; ++r)
     if (e[r] > 1 && e[r] < f.dim[r]) partial = true;
-  if (tp.nTR == 2 && p0 != 0 && e[0] > 1 && e[p0] > 1)
+  if (geom.nTR == 2 && p0 != 0 && e[0] > 1 && e[p0] > 1)
     pd.method = Tiled;
   else if (partial)
     pd.method = PackedSplit;
@@ -535,59 +526,92 @@ void decodeTileHost(const TileParams& tp, uint32_t tile, int64_t& bin, int64_t& 
   }
 }
 
+// In-tile offset of element x numbered in input order (outputSide false)
+// or output order (true), input or output strides.
+int64_t inTileOffset(const TileParams& tp, int x, bool outputSide) {
+  int rem = x;
+  int64_t off = 0;
+  for (int i = 0; i < tp.nTR; ++i) {
+    const int t = outputSide ? tp.trOut[i] : i;
+    const int c = rem % tp.trE[t];
+    rem /= tp.trE[t];
+    off += (int64_t)c * (outputSide ? tp.trSout[t] : tp.trSin[t]);
+  }
+  return off;
+}
+
+// Model of a tile candidate.  DRAM traffic: a tile is tileVol/run runs per
+// side; each run of L bytes starting at byte b touches ((b mod 32) + L + 31)/32
+// sectors, averaged over runs sampled from a few tiles; output runs that
+// start or end inside a sector are partial writes.  Shifted last chunks add
+// their overlap.  Time = the largest of DRAM time, latency-bound time for
+// the bytes in flight, and instruction issue time, plus launch overhead.
 void modelTile(PlanDesc& pd, int numSMs) {
   const Fused& f = pd.f;
   const TileParams& tp = pd.tile;
-  int samples = (int)std::min<int64_t>(8, tp.numTiles);
-  double sectorsIn = 0, sectorsOut = 0, partialOut = 0, useful = 0;
-  std::unordered_set<int64_t> si, so;
-  std::vector<int64_t> outCount;
-  for (int s = 0; s < samples; ++s) {
-    uint32_t tile = (uint32_t)((int64_t)s * tp.numTiles / samples);
+  const int es = f.esize;
+  const RunInfo ri = runOf(f, pd.extent, false), ro = runOf(f, pd.extent, true);
+  const int64_t runIn = ri.run, runOut = ro.run;
+  const int64_t nRunsIn = tp.tileVol / runIn, nRunsOut = tp.tileVol / runOut;
+  const int tilesSampled = (int)std::min<uint32_t>(4, tp.numTiles);
+  double secIn = 0, secOut = 0, partial = 0;
+  int samples = 0;
+  for (int s = 0; s < tilesSampled; ++s) {
+    const uint32_t tile = (uint32_t)((int64_t)s * tp.numTiles / tilesSampled);
     int64_t bin, bout;
     decodeTileHost(tp, tile, bin, bout);
-    si.clear();
-    so.clear();
-    std::unordered_map<int64_t, int> perSector;
-    for (int j = 0; j < tp.tileVol; ++j) {
-      int rem = j;
-      int64_t oi = bin, oo = bout;
-      for (int t = 0; t < tp.nTR; ++t) {
-        int c = rem % tp.trE[t];
-        rem /= tp.trE[t];
-        oi += (int64_t)c * tp.trSin[t];
-        oo += (int64_t)c * tp.trSout[t];
-      }
-      useful += 1;
-      si.insert(oi * f.esize / 32);
-      int64_t sec = oo * f.esize / 32;
-      so.insert(sec);
-      perSector[sec] += f.esize;
+    const int64_t kIn = std::min<int64_t>(nRunsIn, 16), kOut = std::min<int64_t>(nRunsOut, 16);
+    double si = 0, so = 0, pp = 0;
+    for (int64_t k = 0; k < kIn; ++k) {
+      const int64_t b = (bin + inTileOffset(tp, (int)(k * nRunsIn / kIn * runIn), false)) * es;
+      si += (double)(((b & 31) + runIn * es + 31) >> 5);
     }
-    sectorsIn += si.size();
-    sectorsOut += so.size();
-    for (auto& kv : perSector)
-      if (kv.second < 32) partialOut += 1;
+    for (int64_t k = 0; k < kOut; ++k) {
+      const int64_t b = (bout + inTileOffset(tp, (int)(k * nRunsOut / kOut * runOut), true)) * es;
+      const int64_t end = b + runOut * es;
+      so += (double)(((b & 31) + runOut * es + 31) >> 5);
+      pp += ((b & 31) != 0) + ((end & 31) != 0);
+    }
+    secIn += si / kIn * nRunsIn;
+    secOut += so / kOut * nRunsOut;
+    partial += pp / kOut * nRunsOut;
+    ++samples;
   }
-  double scale = (double)tp.numTiles / samples;
-  double dram = (sectorsIn + sectorsOut + partialOut) * 32.0 * scale;
-  double tDram = dram / kBandwidth;
-  int occ = tileCtasPerSM(pd);
-  double conc = (double)numSMs * occ;
-  double active = std::min<double>(conc, tp.numTiles);
-  int ahead = pd.pipe == PIPE_ASYNC ? TILE_STAGES - 1 : 1;
-  if (pd.pipe == PIPE_FLAT) ahead = 1;
-  double inflight = active * ahead * tp.tileVol * f.esize;  // loads in flight
-  double tFlight = (double)f.vol * f.esize / std::max(1.0, inflight) * kLatency;
-  double waves = std::ceil((double)tp.numTiles / conc);
-  double tWaves = waves * 2 * kLatency;
-  // Thread utilisation: slots that carry no element still issue instructions.
-  double util = (double)tp.nIn / (pd.slots * TILE_THREADS);
+  secIn /= samples;
+  secOut /= samples;
+  partial /= samples;
+  const double useful = (double)tp.tileVol * es;
+  pd.effIn = useful / (secIn * 32.0);
+  pd.effOut = useful / (secOut * 32.0);
+  double overlap = 1.0;
+  for (int r = 0; r < f.rank; ++r) {
+    const int64_t nch = ceilDiv(f.dim[r], pd.extent[r]);
+    overlap *= (double)(nch * pd.extent[r]) / (double)f.dim[r];
+  }
+  pd.overlap = overlap;
+  const double dram = (secIn + secOut + partial) * 32.0 * tp.numTiles;
+  const double tDram = dram / kBandwidth;
+  const int occ = tileCtasPerSM(pd);
+  pd.ctasPerSM = occ;
+  const double conc = (double)numSMs * occ;
+  const double active = std::min<double>(conc, tp.numTiles);
+  const int ahead = pd.pipe == PIPE_ASYNC ? TILE_STAGES - 1 : 1;
+  const double inflight = active * ahead * useful;  // loads in flight
+  const double tFlight = (double)f.vol * es * overlap / std::max(1.0, inflight) * kLatency;
+  const double waves = std::ceil((double)tp.numTiles / conc);
+  const double tWaves = waves * 2 * kLatency;
+  const double util = (double)tp.nIn / (pd.slots * TILE_THREADS);
   // instructions per element: ~8 per load unit and ~6 + 2 per element of a
   // store unit, over 4 schedulers x 32 lanes per SM
-  double instPerElem = 8.0 / tp.lv / util + 6.0 / tp.sv + 2.0;
-  double tIssue = (double)f.vol * instPerElem / (numSMs * 128.0 * 1.9e9);
+  const double instPerElem = 8.0 / tp.lv / util + 6.0 / tp.sv + 2.0;
+  const double tIssue = (double)f.vol * overlap * instPerElem / (numSMs * 128.0 * 1.9e9);
+  const long long wf = smemWavefronts(tp, es, tp.padShift, 64);
+  const int sampled = std::min(tp.nIn, 64) + std::min(tp.nOut, 64) * tp.sv;
+  pd.bankPerUnit = sampled > 0 ? (double)wf * 32.0 / sampled : 0.0;
   pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
+  // Measured on the random-shape suite: one-tile-per-CTA launches beat the
+  // persistent pipelines for most shapes at equal modelled traffic.
+  if (pd.pipe == PIPE_FLAT) pd.cost *= 0.9;
 }
 
 void modelRows(PlanDesc& pd, int numSMs) {
@@ -657,12 +681,13 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
         out.push_back(pd);
       }
     }
-    // Tile candidates: (target contiguous run, maximum tile bytes).
-    // (target contiguous run bytes, maximum tile bytes, minimum tile bytes)
+    // Tile candidates: (target contiguous run bytes, maximum tile bytes,
+    // minimum tile bytes), each in the three pipelines.
     const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
                             {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
                             {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
     std::vector<std::vector<int64_t>> seen;
+    const int V = 16 / f.esize;
     for (auto& kb : knobs) {
       int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
       int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
@@ -672,17 +697,15 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
       std::vector<int64_t> key(e, e + f.rank);
       if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
       seen.push_back(key);
+      TileParams geom;
+      if (!buildTileGeometry(f, e, V, V, geom)) continue;
       for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
         PlanDesc pd;
         pd.f = f;
-        pd.pipe = pipe;
         pd.targetRunBytes = kb[0];
         pd.maxTileBytes = kb[1];
-        if (!buildTile(f, e, pd)) continue;
+        if (!buildTile(f, e, pipe, geom, pd)) continue;
         modelTile(pd, numSMs);
-        // Measured on the random-shape suite: one-tile-per-CTA launches beat
-        // the persistent pipelines for most shapes at equal modelled traffic.
-        if (pipe == PIPE_FLAT) pd.cost *= 0.9;
         out.push_back(pd);
       }
     }
@@ -692,6 +715,20 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
     out[i].numCandidates = (int)out.size();
   }
   return out;
+}
+
+bool finalizePlan(PlanDesc& pd) {
+  if (pd.kernel != K_TILE) return true;
+  // element-size units for misaligned pointers, run by the register-staged
+  // pipeline (which builds its own tables)
+  TileParams scalar;
+  if (!buildTileGeometry(pd.f, pd.extent, 1, 1, scalar)) return false;
+  const int smem = tileSmemBytes(scalar, pd.f.esize, PIPE_REG);
+  if (smem > 227 * 1024) return false;
+  pd.tileScalar = scalar;
+  pd.smemBytesScalar = smem;
+  pd.slotsScalar = nextPow2((scalar.nIn + TILE_THREADS - 1) / TILE_THREADS);
+  return true;
 }
 
 int chooseHeuristic(const std::vector<PlanDesc>& cands) {

@@ -139,6 +139,11 @@ struct PlanDesc {
   int candidate = 0;
   int numCandidates = 0;
   int targetRunBytes = 0, maxTileBytes = 0;  // knobs that produced the tile
+  // model statistics (also features of the learned selector)
+  double effIn = 1.0, effOut = 1.0;  // useful bytes / DRAM sector bytes per side
+  double overlap = 1.0;              // elements moved / volume (shifted chunks)
+  double bankPerUnit = 0.0;          // shared wavefronts per 32 sampled accesses
+  int ctasPerSM = 0;                 // modelled occupancy
   TileParams tile{};
   TileParams tileScalar{}; // element-size units (misaligned pointers)
   int slotsScalar = 0, smemBytesScalar = 0;
@@ -163,12 +168,17 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
 // Index of the candidate the analytic model prefers.
 int chooseHeuristic(const std::vector<PlanDesc>& cands);
 
+// Completes a chosen candidate for activation (the element-unit twin of a
+// tile plan, used when pointers are not 16-byte aligned).  False if the
+// twin does not fit.
+bool finalizePlan(PlanDesc& pd);
+
 // Offset tables of a tile (the layout the tile kernels use, see
 // tile_kernel.cuh): ldOff[nIn], stOff[nOut], stSm[tileVol].
 void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short* stSm);
 
-// Shared-memory bank wavefronts of one full tile (load-side writes plus
-// store-side reads) for a given padding; exposed for tests.
-long long smemWavefronts(const TileParams& tp, int esize, int padShift);
+// Shared-memory bank wavefronts of the first sampleUnits load and store
+// units of a tile for a given padding.
+long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits);
 
 }  // namespace lt
