@@ -54,7 +54,9 @@ typedef struct librett_plan_info {
   int grid;                        /* CTAs launched (0 if not yet known)          */
   int candidate;                   /* index into the planner's candidate list     */
   int num_candidates;              /* candidates the planner enumerated           */
-  double model_cost;               /* analytic cost estimate (arbitrary units)    */
+  double model_cost;               /* analytic cost estimate (seconds)            */
+  int selected_by;                 /* 0 analytic model, 1 learned model,
+                                      2 measurement, 3 explicit candidate         */
 } librett_plan_info;
 
 /* librettInitialize / librettFinalize (LibreTT src/librett.h:57,62). */
@@ -110,6 +112,45 @@ int librett_c_plan_candidate(librettHandle* handle, int rank, const int* dim,
 int librett_c_transpose_noalloc(int rank, const int* dim, const int* permutation,
                                 size_t sizeofType, void* stream, const void* idata,
                                 void* odata);
+
+/* ---- Learned plan selection (no LibreTT counterpart; replaces the role of
+ * LibreTT's analytic GpuModel ranking, src/plan.cpp:1073-1643) ---- */
+
+/* Feature vector (nfeatures >= librett_c_mlp_feature_count()) of one
+ * candidate, host-only. */
+int librett_c_candidate_features(int rank, const int* dim, const int* permutation,
+                                 size_t sizeofType, int num_sms, int candidate, float* features,
+                                 int nfeatures);
+
+/* Which model ranks candidates: 0 learned when a model for this device is
+ * loaded else analytic (default), 1 analytic, 2 learned.  Returns the
+ * previous mode, or -1 for an invalid mode.  The LIBRETT_PLAN_SELECTOR
+ * environment variable (auto / analytic / learned) sets the initial mode. */
+int librett_c_set_plan_selector(int mode);
+
+/* Load a weight file (NULL: the default, LIBRETT_PLAN_MODEL or
+ * models/plan_mlp.bin next to the library).  A missing, truncated,
+ * corrupt or non-finite file is rejected and the analytic model stays in
+ * use. */
+int librett_c_load_plan_model(const char* path);
+
+/* MLP sizes and device-pointer kernels used to train the selector on the
+ * GPU (forward with saved activations, backward, MSE gradient, Adam). */
+int librett_c_mlp_param_count(void);
+int librett_c_mlp_feature_count(void);
+int librett_c_mlp_workspace_floats(int batch);
+int librett_c_mlp_forward(const float* params, const float* X, int batch, float* ws, float* out,
+                          void* stream);
+int librett_c_mlp_backward(const float* params, const float* X, int batch, float* ws,
+                           const float* dout, float* grads, void* stream);
+int librett_c_mlp_mse_grad(const float* out, const float* y, int batch, float* dout, float* loss,
+                           void* stream);
+int librett_c_mlp_adam(float* params, const float* grads, float* m, float* v, int n, float lr,
+                       float beta1, float beta2, float eps, int step, void* stream);
+
+/* Host forward pass (standardised inputs, n rows of features) -- the
+ * inference librettPlan runs. */
+int librett_c_mlp_predict_host(const float* params, const float* x, int n, float* out);
 
 /* Number of device kernel launches this library issued since load (all
  * threads, all devices).  Used to count launches inside a timed region. */

@@ -40,6 +40,7 @@ class PlanInfo(ctypes.Structure):
         ("candidate", ctypes.c_int),
         ("num_candidates", ctypes.c_int),
         ("model_cost", ctypes.c_double),
+        ("selected_by", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -66,6 +67,7 @@ class PlanInfo(ctypes.Structure):
             "candidate": self.candidate,
             "num_candidates": self.num_candidates,
             "model_cost": self.model_cost,
+            "selected_by": self.selected_by,
         }
 
 
@@ -90,6 +92,23 @@ C_FUNCTIONS = [
      [ctypes.POINTER(_H), ctypes.c_int, _IP, _IP, ctypes.c_size_t, _P, ctypes.c_int]),
     ("librett_c_transpose_noalloc", ctypes.c_int,
      [ctypes.c_int, _IP, _IP, ctypes.c_size_t, _P, _P, _P]),
+    ("librett_c_candidate_features", ctypes.c_int,
+     [ctypes.c_int, _IP, _IP, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
+      ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    ("librett_c_set_plan_selector", ctypes.c_int, [ctypes.c_int]),
+    ("librett_c_load_plan_model", ctypes.c_int, [ctypes.c_char_p]),
+    ("librett_c_mlp_param_count", ctypes.c_int, []),
+    ("librett_c_mlp_feature_count", ctypes.c_int, []),
+    ("librett_c_mlp_workspace_floats", ctypes.c_int, [ctypes.c_int]),
+    ("librett_c_mlp_forward", ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P, _P]),
+    ("librett_c_mlp_backward", ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P, _P, _P]),
+    ("librett_c_mlp_mse_grad", ctypes.c_int, [_P, _P, ctypes.c_int, _P, _P, _P]),
+    ("librett_c_mlp_adam", ctypes.c_int,
+     [_P, _P, _P, _P, ctypes.c_int, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+      ctypes.c_float, ctypes.c_int, _P]),
+    ("librett_c_mlp_predict_host", ctypes.c_int,
+     [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int,
+      ctypes.POINTER(ctypes.c_float)]),
     ("librett_c_launch_count", ctypes.c_ulonglong, []),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]

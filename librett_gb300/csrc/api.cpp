@@ -12,6 +12,7 @@
 #include <memory>
 #include <mutex>
 #include <shared_mutex>
+#include <string>
 #include <unordered_map>
 #include <vector>
 
@@ -19,6 +20,7 @@
 #include "librett.h"
 #include "librett_c.h"
 #include "plan.h"
+#include "select.h"
 
 namespace lt {
 extern std::atomic<unsigned long long> gLaunchCount;
@@ -28,6 +30,7 @@ namespace {
 
 struct PlanObj {
   lt::PlanDesc pd;
+  int selectedBy = 0;  // librett_plan_info.selected_by
   cudaStream_t stream = nullptr;
   int device = 0;
   int numSMs = 0;
@@ -51,21 +54,27 @@ std::shared_mutex gPlanMu;
 std::unordered_map<librettHandle, std::shared_ptr<PlanObj>> gPlans;
 std::atomic<librettHandle> gNextHandle{0};
 
+struct DevInfo {
+  int sms = 0;
+  std::string name;
+};
 std::mutex gDevMu;
-std::unordered_map<int, int> gDevSMs;
+std::unordered_map<int, DevInfo> gDevs;
 
-bool currentDevice(int& dev, int& sms) {
+bool currentDevice(int& dev, int& sms, std::string* name = nullptr) {
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   std::lock_guard<std::mutex> lk(gDevMu);
-  auto it = gDevSMs.find(dev);
-  if (it != gDevSMs.end()) {
-    sms = it->second;
-    return true;
+  auto it = gDevs.find(dev);
+  if (it == gDevs.end()) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return false;
+    DevInfo di;
+    di.sms = prop.multiProcessorCount;
+    di.name = prop.name;
+    it = gDevs.emplace(dev, di).first;
   }
-  int n = 0;
-  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return false;
-  gDevSMs[dev] = n;
-  sms = n;
+  sms = it->second.sms;
+  if (name) *name = it->second.name;
   return true;
 }
 
@@ -115,11 +124,17 @@ void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   info->model_cost = pd.cost;
 }
 
+void fillInfo(const PlanObj& obj, librett_plan_info* info) {
+  fillInfo(obj.pd, obj.lastGrid, info);
+  info->selected_by = obj.selectedBy;
+}
+
 // Creates the plan object (device tables included) and stores it.
 librettResult activate(librettHandle* handle, const lt::PlanDesc& pd, cudaStream_t stream, int dev,
-                       int sms) {
+                       int sms, int selectedBy) {
   auto obj = std::make_shared<PlanObj>();
   obj->pd = pd;
+  obj->selectedBy = selectedBy;
   obj->stream = stream;
   obj->device = dev;
   obj->numSMs = sms;
@@ -136,15 +151,17 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   if (handle == nullptr) return LIBRETT_INVALID_PARAMETER;
   if (lt::checkInput(rank, dim, perm, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
   int dev = 0, sms = 0;
-  if (!currentDevice(dev, sms)) return LIBRETT_INTERNAL_ERROR;
+  std::string devName;
+  if (!currentDevice(dev, sms, &devName)) return LIBRETT_INTERNAL_ERROR;
   lt::Fused f;
   lt::fuseRanks(rank, dim, perm, (int)sizeofType, f);
   std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
-  int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
+  bool learned = false;
+  int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName.c_str(), &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
   if (!lt::finalizePlan(cands[pick])) return LIBRETT_INTERNAL_ERROR;
-  return activate(handle, cands[pick], stream, dev, sms);
+  return activate(handle, cands[pick], stream, dev, sms, candidate >= 0 ? 3 : (learned ? 1 : 0));
 }
 
 }  // namespace
@@ -224,7 +241,7 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   if (res != LIBRETT_SUCCESS) return res;
-  return activate(handle, cands[best], stream, dev, sms);
+  return activate(handle, cands[best], stream, dev, sms, 2);
 }
 
 librettResult librettDestroy(librettHandle handle) {
@@ -293,7 +310,7 @@ int librett_c_plan_info(librettHandle handle, librett_plan_info* info) {
   if (info == nullptr) return LIBRETT_INVALID_PARAMETER;
   std::shared_ptr<PlanObj> obj = findPlan(handle);
   if (!obj) return LIBRETT_INVALID_PLAN;
-  fillInfo(obj->pd, obj->lastGrid, info);
+  fillInfo(*obj, info);
   return LIBRETT_SUCCESS;
 }
 
@@ -303,11 +320,46 @@ int librett_c_describe(int rank, const int* dim, const int* permutation, size_t 
   if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
   lt::Fused f;
   lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
-  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, num_sms > 0 ? num_sms : 152);
+  const int sms = num_sms > 0 ? num_sms : 152;
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
-  int pick = candidate < 0 ? lt::chooseHeuristic(cands) : candidate;
+  bool learned = false;
+  int pick = candidate < 0 ? lt::choosePlan(cands, sms, nullptr, &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
   fillInfo(cands[pick], 0, info);
+  info->selected_by = candidate >= 0 ? 3 : (learned ? 1 : 0);
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_candidate_features(int rank, const int* dim, const int* permutation,
+                                 size_t sizeofType, int num_sms, int candidate, float* features,
+                                 int nfeatures) {
+  if (features == nullptr || nfeatures < lt::NFEAT) return LIBRETT_INVALID_PARAMETER;
+  if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
+  const int sms = num_sms > 0 ? num_sms : 152;
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  if (candidate < 0 || candidate >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  lt::planFeatures(cands[candidate], sms, features);
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_set_plan_selector(int mode) {
+  if (mode < 0 || mode > 2) return -1;
+  const int prev = lt::selectorMode();
+  lt::setSelectorMode(mode);
+  return prev;
+}
+
+int librett_c_load_plan_model(const char* path) {
+  std::string why;
+  return lt::loadSelectorModel(path, &why) ? LIBRETT_SUCCESS : LIBRETT_INVALID_PARAMETER;
+}
+
+int librett_c_mlp_predict_host(const float* params, const float* x, int n, float* out) {
+  if (params == nullptr || x == nullptr || out == nullptr || n < 0) return LIBRETT_INVALID_PARAMETER;
+  for (int i = 0; i < n; ++i) out[i] = lt::mlpForward(params, x + (size_t)i * lt::NFEAT);
   return LIBRETT_SUCCESS;
 }
 

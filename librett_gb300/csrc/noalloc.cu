@@ -26,6 +26,7 @@
 #include "librett.h"
 #include "librett_c.h"
 #include "plan.h"
+#include "select.h"
 
 namespace lt {
 namespace {
@@ -122,7 +123,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   fuseRanks(rank, dim, permutation, (int)sizeofType, f);
   std::vector<PlanDesc> cands = enumerateCandidates(f, ds.numSMs);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
-  int pick = chooseHeuristic(cands);
+  int pick = choosePlan(cands, ds.numSMs, nullptr, nullptr);
   // Tile problems run the flat pipeline, whose tables go to the scratch.
   if (cands[pick].kernel == K_TILE && cands[pick].pipe != PIPE_FLAT) {
     int flat = -1;

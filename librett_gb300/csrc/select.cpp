@@ -1,0 +1,267 @@
+// Learned plan selection (see select.h).
+#include "select.h"
+
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+
+namespace lt {
+
+namespace {
+
+float lg2(double x) { return (float)std::log2(std::max(x, 1.0)); }
+
+}  // namespace
+
+void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
+  for (int i = 0; i < NFEAT; ++i) out[i] = 0.f;
+  const Fused& f = pd.f;
+  const double vol = (double)f.vol;
+  out[0] = lg2(vol) / 32.f;
+  out[1] = f.esize / 16.f;
+  out[2] = f.rank / 8.f;
+  out[3] = lg2((double)f.dim[0]) / 24.f;
+  out[4] = lg2((double)f.dim[f.perm[0]]) / 24.f;
+  out[5] = f.perm[0] == 0 ? 1.f : 0.f;
+  out[6] = pd.kernel == K_COPY;
+  out[7] = pd.kernel == K_ROW;
+  out[8] = pd.kernel == K_TILE;
+  out[14] = lg2((double)pd.runInBytes) / 20.f;
+  out[15] = lg2((double)pd.runOutBytes) / 20.f;
+  out[16] = pd.unitBytes / 16.f;
+  out[17] = (pd.kernel == K_TILE ? pd.unitOutBytes : pd.unitBytes) / 16.f;
+  out[18] = lg2((double)pd.numWork) / 24.f;
+  out[30] = (float)std::log2(std::max(pd.cost, 1e-7) * 1e6) / 16.f;
+  out[31] = lg2(vol * f.esize) / 36.f;
+  if (pd.kernel != K_TILE) return;
+  const TileParams& tp = pd.tile;
+  out[9] = pd.pipe == PIPE_REG;
+  out[10] = pd.pipe == PIPE_ASYNC;
+  out[11] = pd.pipe == PIPE_FLAT;
+  out[12] = lg2((double)tp.tileVol) / 12.f;
+  out[13] = lg2((double)tp.tileVol * f.esize) / 16.f;
+  out[19] = pd.slots / 16.f;
+  out[20] = pd.smemBytes / (228.f * 1024.f);
+  out[21] = pd.ctasPerSM / 8.f;
+  const double conc = (double)std::max(1, numSMs) * std::max(1, pd.ctasPerSM);
+  out[22] = (float)std::log2(std::max(tp.numTiles / conc, 1e-3) * 8.0) / 16.f;
+  out[23] = tp.nTR / 8.f;
+  out[24] = tp.nGR / 8.f;
+  out[25] = tp.nRagged / 4.f;
+  out[26] = (float)(pd.overlap - 1.0);
+  out[27] = (float)pd.effIn;
+  out[28] = (float)pd.effOut;
+  out[29] = (float)(pd.bankPerUnit / 8.0);
+}
+
+// ---------------------------------------------------------------------------
+// Weight file
+//
+//   char     magic[8]      "LTMLPv01"
+//   uint32   nfeat, hidden, layers, paramCount
+//   int32    sms
+//   char     device[64]    NUL-padded device name
+//   float    mean[nfeat], std[nfeat], ymean, ystd
+//   float    params[paramCount]
+//   uint32   FNV-1a of all preceding bytes
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr char kMagic[8] = {'L', 'T', 'M', 'L', 'P', 'v', '0', '1'};
+
+uint32_t fnv1a(const unsigned char* p, size_t n) {
+  uint32_t h = 2166136261u;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 16777619u;
+  }
+  return h;
+}
+
+}  // namespace
+
+bool loadMlpModel(const std::string& path, MlpModel& m, std::string* why) {
+  auto fail = [&](const char* w) {
+    if (why) *why = w;
+    return false;
+  };
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return fail("cannot open the model file");
+  std::vector<unsigned char> buf((std::istreambuf_iterator<char>(f)),
+                                 std::istreambuf_iterator<char>());
+  const size_t head = 8 + 4 * 4 + 4 + 64;
+  if (buf.size() < head + 4) return fail("model file too short");
+  if (std::memcmp(buf.data(), kMagic, 8) != 0) return fail("bad magic");
+  uint32_t u[4];
+  std::memcpy(u, buf.data() + 8, 16);
+  if (u[0] != (uint32_t)NFEAT || u[1] != (uint32_t)MLP_HIDDEN || u[2] != (uint32_t)MLP_LAYERS ||
+      u[3] != (uint32_t)mlpParamCount())
+    return fail("architecture mismatch");
+  const size_t nfloat = 2 * NFEAT + 2 + mlpParamCount();
+  if (buf.size() != head + 4 * nfloat + 4) return fail("size mismatch");
+  uint32_t sum;
+  std::memcpy(&sum, buf.data() + buf.size() - 4, 4);
+  if (sum != fnv1a(buf.data(), buf.size() - 4)) return fail("checksum mismatch");
+  int32_t sms;
+  std::memcpy(&sms, buf.data() + 24, 4);
+  char dev[65] = {};
+  std::memcpy(dev, buf.data() + 28, 64);
+  std::vector<float> vals(nfloat);
+  std::memcpy(vals.data(), buf.data() + head, 4 * nfloat);
+  for (float v : vals)
+    if (!std::isfinite(v)) return fail("non-finite value");
+  m.sms = sms;
+  m.device = dev;
+  m.mean.assign(vals.begin(), vals.begin() + NFEAT);
+  m.stdv.assign(vals.begin() + NFEAT, vals.begin() + 2 * NFEAT);
+  for (float s : m.stdv)
+    if (!(s > 0.f)) return fail("non-positive feature scale");
+  m.ymean = vals[2 * NFEAT];
+  m.ystd = vals[2 * NFEAT + 1];
+  if (!(m.ystd > 0.f)) return fail("non-positive target scale");
+  m.params.assign(vals.begin() + 2 * NFEAT + 2, vals.end());
+  return true;
+}
+
+float mlpForward(const float* params, const float* x) {
+  float a[MLP_HIDDEN], b[MLP_HIDDEN];
+  const float* w = params;
+  // layer 1: NFEAT -> HIDDEN
+  for (int o = 0; o < MLP_HIDDEN; ++o) {
+    float s = w[MLP_HIDDEN * NFEAT + o];
+    const float* row = w + o * NFEAT;
+    for (int i = 0; i < NFEAT; ++i) s += row[i] * x[i];
+    a[o] = s > 0.f ? s : 0.f;
+  }
+  w += MLP_HIDDEN * NFEAT + MLP_HIDDEN;
+  // layers 2, 3: HIDDEN -> HIDDEN
+  for (int l = 0; l < 2; ++l) {
+    float* src = l == 0 ? a : b;
+    float* dst = l == 0 ? b : a;
+    for (int o = 0; o < MLP_HIDDEN; ++o) {
+      float s = w[MLP_HIDDEN * MLP_HIDDEN + o];
+      const float* row = w + o * MLP_HIDDEN;
+      for (int i = 0; i < MLP_HIDDEN; ++i) s += row[i] * src[i];
+      dst[o] = s > 0.f ? s : 0.f;
+    }
+    w += MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN;
+  }
+  // output: HIDDEN -> 1 (input is `a` after two swaps)
+  float s = w[MLP_HIDDEN];
+  for (int i = 0; i < MLP_HIDDEN; ++i) s += w[i] * a[i];
+  return s;
+}
+
+float mlpPredict(const MlpModel& m, const float* feat) {
+  float x[NFEAT];
+  for (int i = 0; i < NFEAT; ++i) x[i] = (feat[i] - m.mean[i]) / m.stdv[i];
+  return mlpForward(m.params.data(), x) * m.ystd + m.ymean;
+}
+
+// ---------------------------------------------------------------------------
+// Selector state
+// ---------------------------------------------------------------------------
+namespace {
+
+std::mutex gSelMu;
+bool gTried = false;
+bool gLoaded = false;
+MlpModel gModel;
+std::atomic<int> gMode{-1};
+
+int envMode() {
+  const char* e = std::getenv("LIBRETT_PLAN_SELECTOR");
+  if (e == nullptr) return 0;
+  if (std::strcmp(e, "analytic") == 0) return 1;
+  if (std::strcmp(e, "learned") == 0) return 2;
+  return 0;
+}
+
+std::string defaultModelPath() {
+  const char* e = std::getenv("LIBRETT_PLAN_MODEL");
+  if (e != nullptr && *e) return e;
+  Dl_info info;
+  if (dladdr((void*)&defaultModelPath, &info) != 0 && info.dli_fname != nullptr) {
+    std::string so = info.dli_fname;
+    size_t slash = so.rfind('/');
+    std::string dir = slash == std::string::npos ? "." : so.substr(0, slash);
+    return dir + "/models/plan_mlp.bin";
+  }
+  return "models/plan_mlp.bin";
+}
+
+// Caller holds gSelMu.
+void ensureLoaded() {
+  if (gTried) return;
+  gTried = true;
+  MlpModel m;
+  if (loadMlpModel(defaultModelPath(), m, nullptr)) {
+    gModel = std::move(m);
+    gLoaded = true;
+  }
+}
+
+}  // namespace
+
+void setSelectorMode(int mode) { gMode.store(mode); }
+
+int selectorMode() {
+  int m = gMode.load();
+  if (m < 0) {
+    m = envMode();
+    gMode.store(m);
+  }
+  return m;
+}
+
+bool loadSelectorModel(const char* path, std::string* why) {
+  std::lock_guard<std::mutex> lk(gSelMu);
+  if (path == nullptr) {
+    gTried = false;
+    gLoaded = false;
+    ensureLoaded();
+    if (!gLoaded && why) *why = "no model at the default path";
+    return gLoaded;
+  }
+  MlpModel m;
+  if (!loadMlpModel(path, m, why)) return false;
+  gModel = std::move(m);
+  gLoaded = true;
+  gTried = true;
+  return true;
+}
+
+int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
+               bool* usedLearned) {
+  if (usedLearned) *usedLearned = false;
+  const int mode = selectorMode();
+  if (cands.size() <= 1 || mode == 1) return chooseHeuristic(cands);
+  std::lock_guard<std::mutex> lk(gSelMu);
+  ensureLoaded();
+  if (!gLoaded || gModel.sms != numSMs ||
+      (deviceName != nullptr && !gModel.device.empty() && gModel.device != deviceName))
+    return chooseHeuristic(cands);
+  int best = 0;
+  float bestY = 0.f;
+  float feat[NFEAT];
+  for (size_t c = 0; c < cands.size(); ++c) {
+    planFeatures(cands[c], numSMs, feat);
+    const float y = mlpPredict(gModel, feat);
+    if (!std::isfinite(y)) return chooseHeuristic(cands);
+    if (c == 0 || y < bestY) {
+      bestY = y;
+      best = (int)c;
+    }
+  }
+  if (usedLearned) *usedLearned = true;
+  return best;
+}
+
+}  // namespace lt

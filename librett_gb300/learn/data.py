@@ -1,0 +1,139 @@
+"""Problems and per-candidate timings for the learned plan selector.
+
+Problem distribution: rank uniform in 2..7; volume log-uniform in
+2^16..2^28 bytes; element size uniform in {4, 8, 16}; dims drawn
+log-uniformly (random weights summing to log2 volume, each dim >= 2);
+uniformly random permutation.
+
+Timing of one candidate: plan it (librett_c_plan_candidate), one untimed
+launch, then three batches of R back-to-back launches between CUDA events on
+the plan's stream (R chosen so a batch lasts about 100 us, 1 <= R <= 64); the
+time is the median batch time / R.
+
+Usage (on a GPU):
+    python -m librett_gb300.learn.data --problems 6000 --seed 7 --out data.npz
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import sys
+import time
+
+import numpy as np
+
+from .. import _lib
+import librett_gb300 as L
+
+MIN_LOG2_BYTES, MAX_LOG2_BYTES = 16, 28
+
+
+def problems(n: int, seed: int):
+    """n random problems (dims, perm, element bytes) of the selector's distribution."""
+    rng = np.random.Generator(np.random.MT19937(seed))
+    out = []
+    while len(out) < n:
+        rank = int(rng.integers(2, 8))
+        es = int(rng.choice([4, 8, 16]))
+        logbytes = rng.uniform(MIN_LOG2_BYTES, MAX_LOG2_BYTES)
+        logvol = logbytes - np.log2(es)
+        if logvol < rank:  # every dim >= 2
+            continue
+        w = rng.uniform(0.05, 1.0, rank)
+        logd = w / w.sum() * logvol
+        dims = [max(2, int(round(2.0 ** x))) for x in logd]
+        while int(np.prod(dims)) * es > 2 ** MAX_LOG2_BYTES:
+            i = int(np.argmax(dims))
+            dims[i] = max(2, dims[i] // 2)
+        perm = [int(x) for x in rng.permutation(rank)]
+        out.append((dims, perm, es))
+    return out
+
+
+def features(dims, perm, es, candidate, num_sms=152):
+    nf = _lib.load().librett_c_mlp_feature_count()
+    buf = (ctypes.c_float * nf)()
+    rc = _lib.load().librett_c_candidate_features(len(dims), _lib.int_array(dims),
+                                                  _lib.int_array(perm), es, num_sms, candidate,
+                                                  buf, nf)
+    if rc != L.LIBRETT_SUCCESS:
+        raise L.LibrettError(rc, "librett_c_candidate_features")
+    return np.frombuffer(buf, dtype=np.float32).copy()
+
+
+def time_candidate(dims, perm, es, candidate, stream, din, dout, ev):
+    import torch
+
+    plan = L.Plan(dims, perm, es, stream, candidate=candidate)
+    try:
+        nbytes = int(np.prod(dims)) * es
+        est = 2.0 * nbytes / 5e12 + 4e-6
+        reps = int(min(64, max(1, np.ceil(100e-6 / est))))
+        plan.execute(din, dout)
+        ts = []
+        for _ in range(3):
+            ev[0].record(stream)
+            for _ in range(reps):
+                plan.execute(din, dout)
+            ev[1].record(stream)
+            ev[1].synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]) / reps / 1e3)
+        return float(np.median(ts))
+    finally:
+        plan.destroy()
+
+
+def collect(probs, num_sms, log_every=200):
+    """Times every candidate of every problem; returns the dataset dict."""
+    import torch
+
+    stream = torch.cuda.current_stream()
+    maxb = max(int(np.prod(d)) * es for d, _, es in probs)
+    a = torch.empty(maxb, dtype=torch.uint8, device="cuda")
+    b = torch.empty(maxb, dtype=torch.uint8, device="cuda")
+    a.random_(0, 256)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    X, T, P, C = [], [], [], []
+    heur, nbytes = [], []
+    t0 = time.time()
+    for i, (dims, perm, es) in enumerate(probs):
+        h = L.describe(dims, perm, es, num_sms=num_sms)
+        for c in range(h["num_candidates"]):
+            X.append(features(dims, perm, es, c, num_sms))
+            T.append(time_candidate(dims, perm, es, c, stream, a.data_ptr(), b.data_ptr(), ev))
+            P.append(i)
+            C.append(c)
+        heur.append(h["candidate"])  # the analytic model's pick (selector forced to analytic)
+        nbytes.append(int(np.prod(dims)) * es)
+        if log_every and (i + 1) % log_every == 0:
+            print(f"  {i + 1}/{len(probs)} problems, {len(T)} candidates, {time.time() - t0:.0f} s",
+                  flush=True)
+    return {"X": np.array(X, dtype=np.float32), "t": np.array(T), "prob": np.array(P),
+            "cand": np.array(C), "heuristic": np.array(heur), "bytes": np.array(nbytes),
+            "problems": json.dumps(probs)}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--problems", type=int, default=6000)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--out", required=True)
+    args = ap.parse_args(argv)
+    import torch
+
+    torch.cuda.set_device(0)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    prev = _lib.load().librett_c_set_plan_selector(1)  # heuristic picks = the analytic model
+    probs = problems(args.problems, args.seed)
+    data = collect(probs, sms)
+    _lib.load().librett_c_set_plan_selector(prev)
+    data["sms"] = sms
+    data["device"] = torch.cuda.get_device_properties(0).name
+    np.savez_compressed(args.out, **data)
+    print(f"wrote {args.out}: {len(data['t'])} rows, {len(probs)} problems")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

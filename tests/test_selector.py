@@ -1,0 +1,133 @@
+"""Learned plan selection, host side (CPU only): the host inference the
+planner runs, the weight file, its rejection rules and the fallback to the
+analytic model."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+import librett_gb300 as L
+from librett_gb300 import _lib
+from librett_gb300.learn import data as D
+from librett_gb300.learn import train as T
+from oracle import mlp_oracle as M
+
+NF = 32
+
+
+@pytest.fixture
+def restore_selector():
+    lib = _lib.load()
+    prev = lib.librett_c_set_plan_selector(0)
+    lib.librett_c_set_plan_selector(prev)
+    yield lib
+    lib.librett_c_set_plan_selector(prev)
+    lib.librett_c_load_plan_model(None)
+
+
+def _fp(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def test_sizes():
+    lib = _lib.load()
+    assert lib.librett_c_mlp_feature_count() == NF
+    assert lib.librett_c_mlp_param_count() == 128 * NF + 128 + 2 * (128 * 128 + 128) + 128 + 1
+
+
+def test_host_inference_matches_float64_oracle():
+    lib = _lib.load()
+    rng = np.random.default_rng(0)
+    params = T.init_params(NF, rng)
+    params[-129:-1] *= 10  # make the output layer matter
+    X = rng.normal(size=(50, NF)).astype(np.float32)
+    p, pp = _fp(params)
+    x, xp = _fp(X)
+    out = np.zeros(50, dtype=np.float32)
+    assert lib.librett_c_mlp_predict_host(pp, xp, 50,
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+    ref, _ = M.forward(params, X)
+    assert np.allclose(out, ref, rtol=1e-4, atol=1e-4)
+
+
+def test_features_finite_and_deterministic():
+    for dims, perm, es in D.problems(30, seed=3):
+        n = L.describe(dims, perm, es)["num_candidates"]
+        for c in range(n):
+            f1 = D.features(dims, perm, es, c)
+            f2 = D.features(dims, perm, es, c)
+            assert f1.shape == (NF,) and np.all(np.isfinite(f1)) and np.array_equal(f1, f2)
+
+
+def _write(tmp_path, sms=152, device="", corrupt=None):
+    rng = np.random.default_rng(1)
+    params = T.init_params(NF, rng)
+    path = str(tmp_path / "m.bin")
+    T.save_model(path, params, np.zeros(NF, np.float32), np.ones(NF, np.float32), 0.0, 1.0, sms,
+                 device)
+    if corrupt == "byte":
+        raw = bytearray(open(path, "rb").read())
+        raw[200] ^= 0xFF
+        open(path, "wb").write(bytes(raw))
+    elif corrupt == "truncate":
+        raw = open(path, "rb").read()
+        open(path, "wb").write(raw[:-100])
+    elif corrupt == "nan":
+        params[5] = np.nan
+        T.save_model(path, params, np.zeros(NF, np.float32), np.ones(NF, np.float32), 0.0, 1.0,
+                     sms, device)
+    return path, params
+
+
+def test_model_file_round_trip(tmp_path):
+    path, params = _write(tmp_path)
+    m = T.load_model(path)
+    assert np.array_equal(m["params"], params.astype(np.float32))
+
+
+@pytest.mark.parametrize("corrupt", ["byte", "truncate", "nan"])
+def test_bad_model_files_rejected(tmp_path, restore_selector, corrupt):
+    lib = restore_selector
+    path, _ = _write(tmp_path, corrupt=corrupt)
+    assert lib.librett_c_load_plan_model(path.encode()) == L.LIBRETT_INVALID_PARAMETER
+    assert lib.librett_c_load_plan_model(str(tmp_path / "missing.bin").encode()) != 0
+
+
+def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selector):
+    lib = restore_selector
+    dims, perm, es = [64, 48, 32], [2, 0, 1], 4
+    path, _ = _write(tmp_path, sms=152)
+    assert lib.librett_c_load_plan_model(path.encode()) == 0
+    lib.librett_c_set_plan_selector(0)
+    assert L.describe(dims, perm, es, num_sms=152)["selected_by"] == 1
+    # a model for another SM count does not apply
+    assert L.describe(dims, perm, es, num_sms=132)["selected_by"] == 0
+    # forced analytic
+    lib.librett_c_set_plan_selector(1)
+    assert L.describe(dims, perm, es, num_sms=152)["selected_by"] == 0
+    # a single-candidate problem needs no model
+    lib.librett_c_set_plan_selector(2)
+    assert L.describe([5, 7], [0, 1], 8, num_sms=152)["selected_by"] == 0
+    assert lib.librett_c_set_plan_selector(7) == -1
+
+
+def test_learned_pick_is_argmin_of_predictions(tmp_path, restore_selector):
+    lib = restore_selector
+    path, params = _write(tmp_path, sms=152)
+    assert lib.librett_c_load_plan_model(path.encode()) == 0
+    lib.librett_c_set_plan_selector(2)
+    for dims, perm, es in D.problems(10, seed=11):
+        n = L.describe(dims, perm, es)["num_candidates"]
+        X = np.stack([D.features(dims, perm, es, c) for c in range(n)])
+        pred, _ = M.forward(params, X)
+        got = L.describe(dims, perm, es)["candidate"]
+        assert pred[got] <= pred.min() + 1e-4 * max(1.0, abs(pred.min()))
+
+
+def test_targets_relative_and_clipped():
+    t = np.array([1.0, 2.0, 100.0, 3.0, 3.0])
+    prob = np.array([0, 0, 0, 1, 1])
+    y = T.targets(t, prob)
+    assert y[0] == 0 and abs(y[1] - np.log(2)) < 1e-12 and y[2] == T.Y_CLIP and y[3] == y[4] == 0
