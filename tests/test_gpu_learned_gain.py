@@ -1,0 +1,30 @@
+"""What the trained network gains over the analytic model it replaces.
+
+On problems of the selector's distribution drawn with a seed not used in
+training, plans chosen by the learned model (the default when its weight
+file is present) must run faster than plans chosen by the analytic model,
+geomean over the problems, and must not be a large loss on any one of them.
+"""
+import numpy as np
+import pytest
+
+import librett_gb300 as L
+from librett_gb300 import _lib
+from librett_gb300.learn.data import problems
+from librett_gb300.learn.evaluate import evaluate
+
+pytestmark = pytest.mark.gpu
+
+
+def test_learned_choice_beats_analytic(cuda):
+    lib = _lib.load()
+    assert lib.librett_c_load_plan_model(None) == L.LIBRETT_SUCCESS, "weight file missing"
+    # medium and large problems: their timings are stable
+    probs = [p for p in problems(400, seed=97531) if int(np.prod(p[0])) * p[2] >= 1 << 22][:40]
+    summary, rows = evaluate(probs)
+    assert summary["learned_used"] == len(rows)
+    ratio = summary["exec_time_ratio_learned_over_analytic_geomean"]
+    print("learned / analytic execute time, geomean:", ratio)
+    assert ratio < 0.97
+    worst = max(r["exec_ms_learned"] / r["exec_ms_analytic"] for r in rows)
+    assert worst < 1.25
