@@ -128,6 +128,12 @@ int librett_c_candidate_features(int rank, const int* dim, const int* permutatio
  * environment variable (auto / analytic / learned) sets the initial mode. */
 int librett_c_set_plan_selector(int mode);
 
+/* Candidate set: 0 (default) tile plans in the one-tile-per-CTA pipeline
+ * only; 1 also the persistent register-staged and cp.async pipelines (the
+ * LIBRETT_ALL_PIPELINES=1 environment variable sets 1).  Returns the
+ * previous setting.  Changes candidate numbering. */
+int librett_c_set_candidate_set(int all);
+
 /* Load a weight file (NULL: the default, LIBRETT_PLAN_MODEL or
  * models/plan_mlp.bin next to the library).  A missing, truncated,
  * corrupt or non-finite file is rejected and the analytic model stays in

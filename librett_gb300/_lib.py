@@ -95,6 +95,7 @@ C_FUNCTIONS = [
     ("librett_c_candidate_features", ctypes.c_int,
      [ctypes.c_int, _IP, _IP, ctypes.c_size_t, ctypes.c_int, ctypes.c_int,
       ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
+    ("librett_c_set_candidate_set", ctypes.c_int, [ctypes.c_int]),
     ("librett_c_set_plan_selector", ctypes.c_int, [ctypes.c_int]),
     ("librett_c_load_plan_model", ctypes.c_int, [ctypes.c_char_p]),
     ("librett_c_mlp_param_count", ctypes.c_int, []),

@@ -345,6 +345,12 @@ int librett_c_candidate_features(int rank, const int* dim, const int* permutatio
   return LIBRETT_SUCCESS;
 }
 
+int librett_c_set_candidate_set(int all) {
+  const int prev = lt::allPipelines() ? 1 : 0;
+  lt::setAllPipelines(all != 0);
+  return prev;
+}
+
 int librett_c_set_plan_selector(int mode) {
   if (mode < 0 || mode > 2) return -1;
   const int prev = lt::selectorMode();
@@ -359,7 +365,11 @@ int librett_c_load_plan_model(const char* path) {
 
 int librett_c_mlp_predict_host(const float* params, const float* x, int n, float* out) {
   if (params == nullptr || x == nullptr || out == nullptr || n < 0) return LIBRETT_INVALID_PARAMETER;
-  for (int i = 0; i < n; ++i) out[i] = lt::mlpForward(params, x + (size_t)i * lt::NFEAT);
+  // the planner's batched path, with an identity standardisation
+  lt::MlpModel m;
+  m.params.assign(params, params + lt::mlpParamCount());
+  m.prepare();
+  if (n > 0) lt::mlpForwardBatch(m, x, n, out);
   return LIBRETT_SUCCESS;
 }
 

@@ -12,6 +12,8 @@
 #include "plan.h"
 
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
@@ -146,9 +148,10 @@ bool offsetsFit(const Fused& f, const int64_t* e) {
 
 // Extent for a rank of dim d cut into chunks, at most `want` and more than
 // `cur`: prefer a divisor of d (no ragged last chunk) that is a multiple of
-// the 16-byte unit V when d is, within 60% of `want`; else equal chunks.
+// the 16-byte unit V when d is, among the 96 values below `want` and within
+// 60% of it; else equal chunks.
 int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
-  int64_t lo = std::max(cur + 1, (want * 3 + 4) / 5);
+  int64_t lo = std::max(std::max(cur + 1, (want * 3 + 4) / 5), want - 95);
   for (int pass = 0; pass < 2; ++pass) {
     for (int64_t c = want; c >= lo; --c) {
       if (d % c != 0) continue;
@@ -242,71 +245,89 @@ void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short
   }
 }
 
-long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits) {
-  // Simulates the first sampleUnits load units (one per lane) and store
-  // units (one instruction per element of a unit) of a tile.  A phase of
-  // lanes covers 128 bytes; its wavefronts are the largest number of
-  // distinct 4-byte words any bank is asked for.
+namespace {
+
+// Wavefronts of 32-lane accesses: phases of 128 bytes; per phase the largest
+// number of distinct 4-byte words any bank is asked for (a lane touches
+// wordsPerLane consecutive words, so it never hits one bank twice).
+long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
+  long long cost = 0;
+  const int lanesPerPhase = std::max(1, 32 / wordsPerLane);
+  for (int ph = 0; ph < 32; ph += lanesPerPhase) {
+    int words[32][4];
+    int cnt[32] = {};
+    int maxPerBank = 0;
+    for (int l = ph; l < ph + lanesPerPhase; ++l) {
+      if (!act[l]) continue;
+      for (int q = 0; q < wordsPerLane; ++q) {
+        const int wa = addr[l] + q, bk = wa & 31;
+        bool dup = false;
+        for (int k = 0; k < cnt[bk] && k < 4; ++k)
+          if (words[bk][k] == wa) { dup = true; break; }
+        if (dup) continue;
+        if (cnt[bk] < 4) words[bk][cnt[bk]] = wa;
+        if (++cnt[bk] > maxPerBank) maxPerBank = cnt[bk];
+      }
+    }
+    cost += maxPerBank;
+  }
+  return cost;
+}
+
+// Input-order index of the first sampleUnits store units' elements
+// (element m of unit w at [m * n + w]); independent of the padding.
+std::vector<int> storeSample(const TileParams& tp, int sampleUnits, int& n) {
+  n = std::min(tp.nOut, sampleUnits);
+  std::vector<int> j((size_t)n * tp.sv);
+  for (int m = 0; m < tp.sv; ++m)
+    for (int w = 0; w < n; ++w) {
+      int rem = w * tp.sv + m, jj = 0;
+      for (int i = 0; i < tp.nTR; ++i) {
+        const int t = tp.trOut[i];
+        const int c = rem % tp.trE[t];
+        rem /= tp.trE[t];
+        jj += c * tp.trInTile[t];
+      }
+      j[(size_t)m * n + w] = jj;
+    }
+  return j;
+}
+
+long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits,
+                     const std::vector<int>& jStore, int nStore) {
   const int words = esize / 4;
   auto smIdx = [&](int j) { return j + ((j >> padShift) << tp.padLog); };
-  auto jOfQ = [&](int q) {
-    int rem = q, jj = 0;
-    for (int i = 0; i < tp.nTR; ++i) {
-      int t = tp.trOut[i];
-      int c = rem % tp.trE[t];
-      rem /= tp.trE[t];
-      jj += c * tp.trInTile[t];
-    }
-    return jj;
-  };
-  auto phaseCost = [&](const int* addr, const bool* act, int wordsPerLane) {
-    long long cost = 0;
-    const int lanesPerPhase = std::max(1, 32 / wordsPerLane);
-    for (int ph = 0; ph < 32; ph += lanesPerPhase) {
-      // per bank: distinct words (each lane touches wordsPerLane consecutive
-      // words, so one lane never hits a bank twice)
-      int words_[32][4];
-      int cnt[32] = {};
-      int maxPerBank = 0;
-      for (int l = ph; l < ph + lanesPerPhase; ++l) {
-        if (!act[l]) continue;
-        for (int q = 0; q < wordsPerLane; ++q) {
-          const int wa = addr[l] + q, bk = wa & 31;
-          bool dup = false;
-          for (int k = 0; k < cnt[bk] && k < 4; ++k)
-            if (words_[bk][k] == wa) { dup = true; break; }
-          if (dup) continue;
-          if (cnt[bk] < 4) words_[bk][cnt[bk]] = wa;
-          if (++cnt[bk] > maxPerBank) maxPerBank = cnt[bk];
-        }
-      }
-      cost += maxPerBank;
-    }
-    return cost;
-  };
   int addr[32];
   bool act[32];
   long long total = 0;
-  const int nIn = std::min(tp.nIn, sampleUnits), nOut = std::min(tp.nOut, sampleUnits);
+  const int nIn = std::min(tp.nIn, sampleUnits);
   for (int base = 0; base < nIn; base += 32) {
     for (int l = 0; l < 32; ++l) {
-      int u = base + l;
+      const int u = base + l;
       act[l] = u < nIn;
       addr[l] = act[l] ? smIdx(u * tp.lv) * words : 0;
     }
     total += phaseCost(addr, act, words * tp.lv);
   }
-  for (int base = 0; base < nOut; base += 32) {
+  for (int base = 0; base < nStore; base += 32) {
     for (int m = 0; m < tp.sv; ++m) {
       for (int l = 0; l < 32; ++l) {
-        int w = base + l;
-        act[l] = w < nOut;
-        addr[l] = act[l] ? smIdx(jOfQ(w * tp.sv + m)) * words : 0;
+        const int w = base + l;
+        act[l] = w < nStore;
+        addr[l] = act[l] ? smIdx(jStore[(size_t)m * nStore + w]) * words : 0;
       }
       total += phaseCost(addr, act, words);
     }
   }
   return total;
+}
+
+}  // namespace
+
+long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits) {
+  int n = 0;
+  const std::vector<int> j = storeSample(tp, sampleUnits, n);
+  return wavefronts(tp, esize, padShift, sampleUnits, j, n);
 }
 
 namespace {
@@ -411,16 +432,25 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   tp.nOut = tp.tileVol / sv;
   long long best = -1;
   int bestShift = PAD_NONE;
+  // conflict-free lower bound: one wavefront per 128-byte phase
+  const int words = f.esize / 4;
+  const int sIn = std::min(tp.nIn, 64), sOut = std::min(tp.nOut, 64);
+  const long long bound = ((sIn + 31) / 32) * std::max(1, words * lv) +
+                          ((sOut + 31) / 32) * sv * std::max(1, words);
+  int nStore = 0;
+  const std::vector<int> jStore = storeSample(tp, 64, nStore);
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
     if (sh < tp.padLog) continue;
-    long long w = smemWavefronts(tp, f.esize, sh, 64);
+    long long w = wavefronts(tp, f.esize, sh, 64, jStore, nStore);
     if (best < 0 || w < best) {
       best = w;
       bestShift = sh;
     }
+    if (best <= bound) break;
   }
   tp.padShift = bestShift;
+  tp.bankWavefronts = (int)best;
   tp.smStride = tp.tileVol + ((tp.tileVol >> bestShift) << tp.padLog);
   int perVec = 16 / f.esize;
   if (perVec > 1) tp.smStride = (tp.smStride + perVec - 1) / perVec * perVec;
@@ -553,14 +583,14 @@ void modelTile(PlanDesc& pd, int numSMs) {
   const RunInfo ri = runOf(f, pd.extent, false), ro = runOf(f, pd.extent, true);
   const int64_t runIn = ri.run, runOut = ro.run;
   const int64_t nRunsIn = tp.tileVol / runIn, nRunsOut = tp.tileVol / runOut;
-  const int tilesSampled = (int)std::min<uint32_t>(4, tp.numTiles);
+  const int tilesSampled = (int)std::min<uint32_t>(2, tp.numTiles);
   double secIn = 0, secOut = 0, partial = 0;
   int samples = 0;
   for (int s = 0; s < tilesSampled; ++s) {
     const uint32_t tile = (uint32_t)((int64_t)s * tp.numTiles / tilesSampled);
     int64_t bin, bout;
     decodeTileHost(tp, tile, bin, bout);
-    const int64_t kIn = std::min<int64_t>(nRunsIn, 16), kOut = std::min<int64_t>(nRunsOut, 16);
+    const int64_t kIn = std::min<int64_t>(nRunsIn, 8), kOut = std::min<int64_t>(nRunsOut, 8);
     double si = 0, so = 0, pp = 0;
     for (int64_t k = 0; k < kIn; ++k) {
       const int64_t b = (bin + inTileOffset(tp, (int)(k * nRunsIn / kIn * runIn), false)) * es;
@@ -605,7 +635,7 @@ void modelTile(PlanDesc& pd, int numSMs) {
   // store unit, over 4 schedulers x 32 lanes per SM
   const double instPerElem = 8.0 / tp.lv / util + 6.0 / tp.sv + 2.0;
   const double tIssue = (double)f.vol * overlap * instPerElem / (numSMs * 128.0 * 1.9e9);
-  const long long wf = smemWavefronts(tp, es, tp.padShift, 64);
+  const long long wf = tp.bankWavefronts;
   const int sampled = std::min(tp.nIn, 64) + std::min(tp.nOut, 64) * tp.sv;
   pd.bankPerUnit = sampled > 0 ? (double)wf * 32.0 / sampled : 0.0;
   pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
@@ -645,6 +675,22 @@ void modelRows(PlanDesc& pd, int numSMs) {
 }
 
 }  // namespace
+
+namespace {
+std::atomic<int> gAllPipelines{-1};
+}
+
+void setAllPipelines(bool all) { gAllPipelines.store(all ? 1 : 0); }
+
+bool allPipelines() {
+  int v = gAllPipelines.load();
+  if (v < 0) {
+    const char* e = std::getenv("LIBRETT_ALL_PIPELINES");
+    v = (e != nullptr && e[0] == '1') ? 1 : 0;
+    gAllPipelines.store(v);
+  }
+  return v == 1;
+}
 
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
   std::vector<PlanDesc> out;
@@ -699,7 +745,9 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
       seen.push_back(key);
       TileParams geom;
       if (!buildTileGeometry(f, e, V, V, geom)) continue;
+      const bool all = allPipelines();
       for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
+        if (pipe != PIPE_FLAT && !all) continue;
         PlanDesc pd;
         pd.f = f;
         pd.targetRunBytes = kb[0];

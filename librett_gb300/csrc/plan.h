@@ -88,6 +88,7 @@ struct TileParams {
   int padShift;         // smem index = j + ((j >> padShift) << padLog); PAD_NONE = none
   int smStride;         // elements per smem buffer including padding
   int nRagged;          // grid ranks whose dim is not a multiple of the extent
+  int bankWavefronts;   // planner only: simulated wavefronts at padShift
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
@@ -162,8 +163,13 @@ int checkInput(int rank, const int* dim, const int* perm, size_t sizeofType);
 void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
 
 // Candidate plans for a fused problem on a device with numSMs SMs.  The
-// first entry is never empty.  Each candidate's `cost` is filled in.
+// first entry is never empty.  Each candidate's `cost` is filled in.  By
+// default tile candidates use the flat pipeline only (it wins on nearly all
+// measured problems); setAllPipelines(true) or LIBRETT_ALL_PIPELINES=1 adds
+// the persistent register-staged and cp.async variants.
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
+void setAllPipelines(bool all);
+bool allPipelines();
 
 // Index of the candidate the analytic model prefers.
 int chooseHeuristic(const std::vector<PlanDesc>& cands);

@@ -127,6 +127,7 @@ bool loadMlpModel(const std::string& path, MlpModel& m, std::string* why) {
   m.ystd = vals[2 * NFEAT + 1];
   if (!(m.ystd > 0.f)) return fail("non-positive target scale");
   m.params.assign(vals.begin() + 2 * NFEAT + 2, vals.end());
+  m.prepare();
   return true;
 }
 
@@ -157,6 +158,60 @@ float mlpForward(const float* params, const float* x) {
   float s = w[MLP_HIDDEN];
   for (int i = 0; i < MLP_HIDDEN; ++i) s += w[i] * a[i];
   return s;
+}
+
+void MlpModel::prepare() {
+  auto transpose = [](const float* w, int out, int in, std::vector<float>& t) {
+    t.resize((size_t)out * in);
+    for (int o = 0; o < out; ++o)
+      for (int i = 0; i < in; ++i) t[(size_t)i * out + o] = w[(size_t)o * in + i];
+  };
+  const float* w = params.data();
+  transpose(w, MLP_HIDDEN, NFEAT, wt1);
+  w += MLP_HIDDEN * NFEAT + MLP_HIDDEN;
+  transpose(w, MLP_HIDDEN, MLP_HIDDEN, wt2);
+  w += MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN;
+  transpose(w, MLP_HIDDEN, MLP_HIDDEN, wt3);
+}
+
+namespace {
+
+// y[r][o] = relu(b[o] + sum_i x[r][i] * wt[i][o]) for r < n.  The input
+// index is the outer loop so each weight row is read once for all rows
+// (the weights do not fit in L1; the n output rows do).
+void denseRelu(const float* x, int n, int in, const float* wt, const float* b, float* y) {
+  for (int r = 0; r < n; ++r)
+    for (int o = 0; o < MLP_HIDDEN; ++o) y[(size_t)r * MLP_HIDDEN + o] = b[o];
+  for (int i = 0; i < in; ++i) {
+    const float* wi = wt + (size_t)i * MLP_HIDDEN;
+    for (int r = 0; r < n; ++r) {
+      const float xi = x[(size_t)r * in + i];
+      float* yr = y + (size_t)r * MLP_HIDDEN;
+      for (int o = 0; o < MLP_HIDDEN; ++o) yr[o] += xi * wi[o];
+    }
+  }
+  for (size_t k = 0; k < (size_t)n * MLP_HIDDEN; ++k) y[k] = y[k] > 0.f ? y[k] : 0.f;
+}
+
+}  // namespace
+
+void mlpForwardBatch(const MlpModel& m, const float* x, int n, float* out) {
+  std::vector<float> a((size_t)n * MLP_HIDDEN), b((size_t)n * MLP_HIDDEN);
+  const float* p = m.params.data();
+  const float* b1 = p + MLP_HIDDEN * NFEAT;
+  const float* b2 = b1 + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN;
+  const float* b3 = b2 + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN;
+  const float* w4 = b3 + MLP_HIDDEN;
+  const float b4 = w4[MLP_HIDDEN];
+  denseRelu(x, n, NFEAT, m.wt1.data(), b1, a.data());
+  denseRelu(a.data(), n, MLP_HIDDEN, m.wt2.data(), b2, b.data());
+  denseRelu(b.data(), n, MLP_HIDDEN, m.wt3.data(), b3, a.data());
+  for (int r = 0; r < n; ++r) {
+    const float* ar = a.data() + (size_t)r * MLP_HIDDEN;
+    float s = 0.f;
+    for (int i = 0; i < MLP_HIDDEN; ++i) s += w4[i] * ar[i];
+    out[r] = s + b4;
+  }
 }
 
 float mlpPredict(const MlpModel& m, const float* feat) {
@@ -248,17 +303,18 @@ int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* devic
   if (!gLoaded || gModel.sms != numSMs ||
       (deviceName != nullptr && !gModel.device.empty() && gModel.device != deviceName))
     return chooseHeuristic(cands);
+  const int n = (int)cands.size();
+  std::vector<float> x((size_t)n * NFEAT), y(n);
+  for (int c = 0; c < n; ++c) {
+    float* xc = x.data() + (size_t)c * NFEAT;
+    planFeatures(cands[c], numSMs, xc);
+    for (int i = 0; i < NFEAT; ++i) xc[i] = (xc[i] - gModel.mean[i]) / gModel.stdv[i];
+  }
+  mlpForwardBatch(gModel, x.data(), n, y.data());
   int best = 0;
-  float bestY = 0.f;
-  float feat[NFEAT];
-  for (size_t c = 0; c < cands.size(); ++c) {
-    planFeatures(cands[c], numSMs, feat);
-    const float y = mlpPredict(gModel, feat);
-    if (!std::isfinite(y)) return chooseHeuristic(cands);
-    if (c == 0 || y < bestY) {
-      bestY = y;
-      best = (int)c;
-    }
+  for (int c = 0; c < n; ++c) {
+    if (!std::isfinite(y[c])) return chooseHeuristic(cands);
+    if (y[c] < y[best]) best = c;
   }
   if (usedLearned) *usedLearned = true;
   return best;

@@ -35,7 +35,15 @@ struct MlpModel {
   std::vector<float> mean, stdv;  // feature standardisation
   float ymean = 0.f, ystd = 1.f;  // target de-standardisation
   std::vector<float> params;      // mlpParamCount() floats
+  // hidden-layer weights transposed to [in][out] for the batched forward
+  std::vector<float> wt1, wt2, wt3;
+  void prepare();                 // fills wt1..wt3 from params
 };
+
+// Batched forward of n standardised feature rows (the planner's hot path):
+// out[r] = network output.  Inner loops run over contiguous outputs, so the
+// compiler vectorises them without reassociating sums.
+void mlpForwardBatch(const MlpModel& m, const float* x, int n, float* out);
 
 // Reads a weight file; false (with a reason) if the magic, version, sizes,
 // checksum or any value (NaN / Inf) is wrong.

@@ -125,6 +125,7 @@ def main(argv=None):
     torch.cuda.set_device(0)
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     prev = _lib.load().librett_c_set_plan_selector(1)  # heuristic picks = the analytic model
+    _lib.load().librett_c_set_candidate_set(1)  # time every pipeline
     probs = problems(args.problems, args.seed)
     data = collect(probs, sms)
     _lib.load().librett_c_set_plan_selector(prev)
