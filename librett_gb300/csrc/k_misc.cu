@@ -84,36 +84,77 @@ cudaError_t launchRowsUnit(int unit, const RowParams& rp, const void* in, void* 
 
 }  // namespace
 
+__global__ void __launch_bounds__(256)
+writeTileTablesKernel(const __grid_constant__ TileParams p, int* ldOff, int* stOff,
+                      unsigned short* stSm) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < p.nIn; u += stride) {
+    int rem = u * p.lv, off = 0;
+    for (int t = 0; t < p.nTR; ++t) {
+      const int e = p.trE[t];
+      const int q = rem / e;
+      off += (rem - q * e) * p.trSin[t];
+      rem = q;
+    }
+    ldOff[u] = off;
+  }
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.tileVol; q += stride) {
+    int rem = q, off = 0, jj = 0;
+    for (int i = 0; i < p.nTR; ++i) {
+      const int t = p.trOut[i];
+      const int e = p.trE[t];
+      const int d = rem / e;
+      const int c = rem - d * e;
+      rem = d;
+      off += c * p.trSout[t];
+      jj += c * p.trInTile[t];
+    }
+    stSm[q] = (unsigned short)(jj + ((jj >> p.padShift) << p.padLog));
+    if (q % p.sv == 0) stOff[q / p.sv] = off;
+  }
+}
+
+size_t deviceTableBytes(const TileParams& tp, size_t* stOffset, size_t* smOffset) {
+  // stSm is read 4 or 8 bytes at a time by the store gathers: keep it
+  // 16-byte aligned
+  *stOffset = 4 * (size_t)tp.nIn;
+  *smOffset = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16;
+  return *smOffset + 2 * (size_t)tp.tileVol;
+}
+
+cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStream_t s,
+                              DeviceTables* dt) {
+  size_t stOffset, smOffset;
+  deviceTableBytes(tp, &stOffset, &smOffset);
+  int* ld = reinterpret_cast<int*>(base);
+  int* st = reinterpret_cast<int*>(base + stOffset);
+  unsigned short* sm = reinterpret_cast<unsigned short*>(base + smOffset);
+  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(tp, ld, st, sm);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  dt->ldOff = ld;
+  dt->stOff = st;
+  dt->stSm = sm;
+  return cudaSuccess;
+}
+
 cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt) {
   *alloc = nullptr;
   *dt = DeviceTables();
   if (pd.kernel != K_TILE || pd.pipe != PIPE_FLAT) return cudaSuccess;
-  const TileParams& tp = pd.tile;
-  const size_t ldBytes = 4 * (size_t)tp.nIn;
-  // stSm is read 4 or 8 bytes at a time by the store gathers: keep it
-  // 16-byte aligned
-  const size_t stBytes = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16 - ldBytes;
-  const size_t smBytes = 2 * (size_t)tp.tileVol;
-  const size_t total = ldBytes + stBytes + smBytes;
-  std::vector<unsigned char> host(total);
-  int* ld = reinterpret_cast<int*>(host.data());
-  int* st = reinterpret_cast<int*>(host.data() + ldBytes);
-  unsigned short* sm = reinterpret_cast<unsigned short*>(host.data() + ldBytes + stBytes);
-  tileTablesHost(tp, ld, st, sm);
+  size_t stOffset, smOffset;
+  const size_t total = deviceTableBytes(pd.tile, &stOffset, &smOffset);
   void* d = nullptr;
   cudaError_t err = cudaMallocAsync(&d, total, s);
   if (err != cudaSuccess) return err;
-  // pageable source: the call returns once the bytes have been staged
-  err = cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s);
+  // the tables are computed on the device, in stream order before any use
+  err = writeDeviceTables(pd.tile, static_cast<unsigned char*>(d), s, dt);
   if (err != cudaSuccess) {
     cudaFreeAsync(d, s);
+    *dt = DeviceTables();
     return err;
   }
   *alloc = d;
-  unsigned char* b = static_cast<unsigned char*>(d);
-  dt->ldOff = reinterpret_cast<const int*>(b);
-  dt->stOff = reinterpret_cast<const int*>(b + ldBytes);
-  dt->stSm = reinterpret_cast<const unsigned short*>(b + ldBytes + stBytes);
   return cudaSuccess;
 }
 

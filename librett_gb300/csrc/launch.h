@@ -23,6 +23,15 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
 // Releases them in stream order (cudaFreeAsync on s).
 void destroyDeviceTables(void* alloc, cudaStream_t s);
 
+// Device-table layout of a tile: total bytes; ldOff at 0, stOff at
+// *stOffset, stSm at *smOffset (16-byte aligned).
+size_t deviceTableBytes(const TileParams& tp, size_t* stOffset, size_t* smOffset);
+
+// Launches a kernel on s that writes the tables of tp at base (which must
+// hold deviceTableBytes), and points *dt at them.
+cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStream_t s,
+                              DeviceTables* dt);
+
 // Launch whatever the plan describes on stream s.  Uses the 16-byte unit
 // variant when both pointers allow it, else the element-size one.  *grid
 // receives the number of CTAs launched.  dt: the plan's device tables (flat

@@ -11,8 +11,8 @@
 // How: the flat tile kernel reads its offset tables from global memory.
 // Here those tables live in a fixed file-scope device array (every GPU that
 // loads the library holds it until the process exits).  A small kernel
-// writes the tables of the current problem into it, then the transpose runs
-// on them, both on the caller's stream.  Host code cannot use the array's
+// (writeDeviceTables) writes the tables of the current problem into it, then
+// the transpose runs on them, both on the caller's stream.  Host code cannot use the array's
 // name as a device address; its address is obtained per device with
 // cudaGetSymbolAddress on the first call made with that device current.
 #include <cuda_runtime.h>
@@ -37,40 +37,6 @@ namespace {
 constexpr size_t kScratchBytes = 64 * 1024;
 
 __device__ __align__(256) unsigned char gTableScratch[kScratchBytes];
-
-// Writes the offset tables of tile p (the layout of createDeviceTables):
-// ldOff[nIn], stOff[nOut] (the two padded to 16 bytes), stSm[tileVol].
-__global__ void __launch_bounds__(256)
-writeTablesKernel(const __grid_constant__ TileParams p, size_t stOffset, size_t smOffset) {
-  int* ldOff = reinterpret_cast<int*>(gTableScratch);
-  int* stOff = reinterpret_cast<int*>(gTableScratch + stOffset);
-  unsigned short* stSm = reinterpret_cast<unsigned short*>(gTableScratch + smOffset);
-  const int stride = gridDim.x * blockDim.x;
-  for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < p.nIn; u += stride) {
-    int rem = u * p.lv, off = 0;
-    for (int t = 0; t < p.nTR; ++t) {
-      const int e = p.trE[t];
-      const int q = rem / e;
-      off += (rem - q * e) * p.trSin[t];
-      rem = q;
-    }
-    ldOff[u] = off;
-  }
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < p.tileVol; q += stride) {
-    int rem = q, off = 0, jj = 0;
-    for (int i = 0; i < p.nTR; ++i) {
-      const int t = p.trOut[i];
-      const int e = p.trE[t];
-      const int d = rem / e;
-      const int c = rem - d * e;
-      rem = d;
-      off += c * p.trSout[t];
-      jj += c * p.trInTile[t];
-    }
-    stSm[q] = (unsigned short)(jj + ((jj >> p.padShift) << p.padLog));
-    if (q % p.sv == 0) stOff[q / p.sv] = off;
-  }
-}
 
 struct DeviceScratch {
   unsigned char* ptr = nullptr;
@@ -139,16 +105,10 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   const bool vecOk = ((uintptr_t)idata % 16 == 0 && (uintptr_t)odata % 16 == 0) ||
                      (pd.tile.lv == 1 && pd.tile.sv == 1);
   if (pd.kernel == K_TILE && pd.pipe == PIPE_FLAT && vecOk) {
-    const TileParams& tp = pd.tile;
-    const size_t stOffset = 4 * (size_t)tp.nIn;
-    const size_t smOffset = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16;
-    const size_t need = smOffset + 2 * (size_t)tp.tileVol;
-    if (need > kScratchBytes) return LIBRETT_INVALID_PARAMETER;  // tables exceed the scratch
-    writeTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(tp, stOffset, smOffset);
-    if (cudaGetLastError() != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
-    dt.ldOff = reinterpret_cast<const int*>(ds.ptr);
-    dt.stOff = reinterpret_cast<const int*>(ds.ptr + stOffset);
-    dt.stSm = reinterpret_cast<const unsigned short*>(ds.ptr + smOffset);
+    size_t stOffset, smOffset;
+    if (deviceTableBytes(pd.tile, &stOffset, &smOffset) > kScratchBytes)
+      return LIBRETT_INVALID_PARAMETER;  // tables exceed the scratch
+    if (writeDeviceTables(pd.tile, ds.ptr, s, &dt) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   }
   int grid = 0;
   if (launchPlan(pd, &dt, idata, odata, s, ds.numSMs, &grid) != cudaSuccess)

@@ -11,6 +11,7 @@ Usage (on a GPU):
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import sys
 import time
@@ -44,6 +45,7 @@ def evaluate(probs):
 
     lib = _lib.load()
     stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
     maxb = max(int(np.prod(d)) * es for d, _, es in probs)
     a = torch.empty(maxb, dtype=torch.uint8, device="cuda")
     b = torch.empty(maxb, dtype=torch.uint8, device="cuda")
@@ -54,22 +56,32 @@ def evaluate(probs):
     try:
         for dims, perm, es in probs:
             r = {"dims": dims, "perm": perm, "es": es}
+            dims_c, perm_c = _lib.int_array(dims), _lib.int_array(perm)
             for mode, name in ((1, "analytic"), (2, "learned")):
                 lib.librett_c_set_plan_selector(mode)
                 torch.cuda.synchronize()
+                # the C-ABI call alone (what a C/C++ caller pays)
+                h = ctypes.c_uint(0)
                 t0 = time.perf_counter()
-                plan = L.Plan(dims, perm, es, stream)
+                rc = lib.librett_c_plan(ctypes.byref(h), len(dims), dims_c, perm_c, es, sptr)
                 r[f"plan_ms_{name}"] = (time.perf_counter() - t0) * 1e3
+                assert rc == 0
+                lib.librett_c_destroy(h.value)
+                plan = L.Plan(dims, perm, es, stream)
                 info = plan.info()
                 r[f"selected_by_{name}"] = info["selected_by"]
                 r[f"candidate_{name}"] = info["candidate"]
                 r[f"exec_ms_{name}"] = _time_exec(plan, a.data_ptr(), b.data_ptr(), stream, ev) * 1e3
                 plan.destroy()
             torch.cuda.synchronize()
+            h = ctypes.c_uint(0)
             t0 = time.perf_counter()
-            plan = L.Plan(dims, perm, es, stream, measure=(a.data_ptr(), b.data_ptr()))
-            torch.cuda.synchronize()
+            rc = lib.librett_c_plan_measure(ctypes.byref(h), len(dims), dims_c, perm_c, es, sptr,
+                                            a.data_ptr(), b.data_ptr())
             r["plan_ms_measure"] = (time.perf_counter() - t0) * 1e3
+            assert rc == 0
+            lib.librett_c_destroy(h.value)
+            plan = L.Plan(dims, perm, es, stream, measure=(a.data_ptr(), b.data_ptr()))
             r["exec_ms_measure"] = _time_exec(plan, a.data_ptr(), b.data_ptr(), stream, ev) * 1e3
             plan.destroy()
             rows.append(r)
@@ -88,6 +100,16 @@ def evaluate(probs):
     }
     summary["plan_latency_measure_over_learned"] = (summary["plan_ms_median"]["measure"] /
                                                     summary["plan_ms_median"]["learned"])
+    # by problem size
+    buckets = {}
+    for lo, hi in ((16, 20), (20, 24), (24, 29)):
+        sel = [r for r in rows if lo <= np.log2(np.prod(r["dims"]) * r["es"]) < hi]
+        if sel:
+            buckets[f"2^{lo}..2^{hi} bytes"] = {
+                "problems": len(sel),
+                "learned_ms": float(np.median([r["plan_ms_learned"] for r in sel])),
+                "measure_ms": float(np.median([r["plan_ms_measure"] for r in sel]))}
+    summary["by_size"] = buckets
     return summary, rows
 
 
