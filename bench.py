@@ -70,6 +70,8 @@ WORKLOADS = {
     "c3b": "float32 dims (2,3,4,5,65536,16) perm (5,3,1,4,0,2)",
     "c1": "float32 dims (64,48,32) perm (2,0,1)",
     "custom": "one problem given by --dims/--perm/--es",
+    "grouped": "batched grouped execute: 10,000 transposes, rank 2..6, volume log-uniform "
+               "2^10..2^22 elements, float32/float64 50/50, random permutations",
 }
 
 
@@ -84,6 +86,9 @@ def workload_problems(name, nproblems, custom=None):
         return [([2, 3, 4, 5, 65536, 16], [5, 3, 1, 4, 0, 2], 4)]
     if name == "c1":
         return [([64, 48, 32], [2, 0, 1], 4)]
+    if name == "grouped":
+        from librett_gb300.workloads import grouped_problems
+        return grouped_problems(nproblems)
     raise ValueError(name)
 
 
@@ -218,6 +223,40 @@ def cpu_gather_time(problems, budget_s, threads, rng_seed=1):
     return bytes_total / t_total / 1e9, done, t_total
 
 
+GROUP_SLICE = 100  # problems per reference-arm step of the grouped workload
+
+
+def _reference_grouped(args, problems, threads):
+    """Reference arm of the grouped workload: the oracle's host gather over
+    consecutive slices of GROUP_SLICE problems, one slice per step."""
+    t_all, n_all, b_all = 0.0, 0, 0
+    for i in range(args.steps):
+        lo = ((args.warmup + i) * GROUP_SLICE) % len(problems)
+        sl = problems[lo:lo + GROUP_SLICE]
+        _, n, t = cpu_gather_time(sl, float("inf"), threads)
+        t_all += t
+        n_all += n
+        b_all += sum(2 * problem_bytes(p) for p in sl[:n])
+    value = n_all / t_all
+    line = {
+        "impl": "reference", "metric": "transposes/s (grouped)", "value": round(value, 1),
+        "unit": "transposes/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t_all / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64",
+        "data": "synthetic random bit patterns",
+        "config": {"workload": WORKLOADS["grouped"], "problems_per_step": GROUP_SLICE,
+                   "parallelism": "host threads"},
+        "gbs": round(b_all / t_all / 1e9, 3),
+        "cpu_baseline": {"value": round(value, 1), "unit": "transposes/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{GROUP_SLICE} consecutive problems per step, {args.steps} steps"},
+        "e2e": {"value": round(value, 1), "unit": "transposes/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, _, world = dist_setup(args.gpus)
     problems = workload_problems(args.workload, args.problems, args.custom)
@@ -229,6 +268,8 @@ def run_reference(args):
     # warm-up steps: one problem each
     for i in range(args.warmup):
         cpu_gather_time([problems[i % len(problems)]], 0.0, threads)
+    if args.workload == "grouped":
+        return _reference_grouped(args, problems, threads)
     gbs_t, bytes_t = 0.0, 0
     t_all = 0.0
     for i in range(args.steps):
@@ -432,6 +473,186 @@ def run_engine(args):
     return 0
 
 
+def run_grouped(args):
+    """Grouped workload: one step = one execution of a group of all the
+    problems (one CUDA graph), each tensor at its own 256-byte-aligned offset
+    of one input and one output buffer.  The plain per-tensor loop
+    (librettExecute on every plan, one launch each) is timed on the same
+    buffers in its own region."""
+    import torch
+
+    import librett_gb300 as L
+    from librett_gb300.workloads import GROUPED_SEED, packed_offsets
+
+    rank, local, world = dist_setup(args.gpus)
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    problems = workload_problems("grouped", args.problems)
+    n = len(problems)
+    offs, total = packed_offsets(problems)
+    stream = torch.cuda.current_stream(dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4321 + rank)
+    inp = torch.randint(-(2 ** 62), 2 ** 62, (total // 8,), dtype=torch.int64, device=dev,
+                        generator=g).view(torch.uint8)
+    out = torch.empty(total, dtype=torch.uint8, device=dev)
+    ins = [inp.data_ptr() + o for o in offs]
+    outs = [out.data_ptr() + o for o in offs]
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    plans = [L.Plan(d, p, es, stream) for d, p, es in problems]
+    plan_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    grp = L.Group(plans, ins, outs, stream)
+    create_s = time.perf_counter() - t0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def time_group(k):
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(k):
+            grp.execute()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        return e0.elapsed_time(e1) / k
+
+    # the plan selector's tiles, then the autotuned tile policy (tuning is a
+    # one-time cost per batch signature, outside the timed region)
+    grp.execute()
+    untuned_ms = time_group(max(1, args.steps))
+    tune_s = None
+    if not args.no_tune:
+        t0 = time.perf_counter()
+        grp.tune()
+        tune_s = time.perf_counter() - t0
+    policy, tuned = grp.policy()
+    ginfo = grp.info()
+    step_bytes = ginfo["bytes"]
+
+    for _ in range(args.warmup):
+        grp.execute()
+        L.execute_batch(plans, ins, outs)
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    launches0 = L.launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        grp.execute()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    launches = L.launch_count() - launches0
+    barrier(world)
+    clk = clocks.stop()
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+
+    # the plain per-tensor loop on the same buffers
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    e0.record(stream)
+    for _ in range(args.steps):
+        L.execute_batch(plans, ins, outs)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    loop_ms = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+
+    value = world * n / (ms / 1e3)
+    gbs = step_bytes / (ms / 1e3) / 1e9
+    loop_value = world * n / (loop_ms / 1e3)
+    peak, peak_kind = load_peaks()
+
+    # end to end on a prefix of the batch whose inputs fit 2 GiB of pinned
+    # host memory: H2D of the inputs, the group, D2H of the outputs
+    e2e = None
+    if not args.no_e2e:
+        cap, m = 2 << 30, 0
+        while m < n and offs[m] + problem_bytes(problems[m]) <= cap:
+            m += 1
+        sub_bytes = offs[m - 1] + problem_bytes(problems[m - 1])
+        hin = torch.empty(sub_bytes, dtype=torch.uint8, pin_memory=True)
+        hin.copy_(inp[:sub_bytes].cpu())
+        hout = torch.empty(sub_bytes, dtype=torch.uint8, pin_memory=True)
+        with L.Group(plans[:m], ins[:m], outs[:m], stream, policy=policy) as sub:
+            def e2e_step():
+                inp[:sub_bytes].copy_(hin, non_blocking=True)
+                sub.execute()
+                hout.copy_(out[:sub_bytes], non_blocking=True)
+
+            for _ in range(2):
+                e2e_step()
+            torch.cuda.synchronize(dev)
+            barrier(world)
+            e0.record(stream)
+            for _ in range(args.steps):
+                e2e_step()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ems = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+        e2e = {"value": round(world * m / (ems / 1e3), 1), "unit": "transposes/s",
+               "h2d_bytes_per_step": sub_bytes, "d2h_bytes_per_step": sub_bytes,
+               "ms_per_step": round(ems, 3), "members": m,
+               "note": f"first {m} problems of the batch (inputs within 2 GiB of pinned host "
+                       "memory), one H2D and one D2H copy of the packed buffers per step"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        _, done, t = cpu_gather_time(problems, args.cpu_budget, host_threads())
+        cpu = {"value": round(done / t, 1), "unit": "transposes/s", "cores": host_threads(),
+               "kind": "port", "sample": f"first {done} problems of the batch, {t:.1f} s of "
+                                         "host gather"}
+    grp.destroy()
+    for pl in plans:
+        pl.destroy()
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "transposes/s (grouped)",
+        "value": round(value, 1),
+        "unit": "transposes/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "u32/u64",
+        "data": "synthetic random 64-bit patterns, fixed seeds",
+        "config": {"workload": WORKLOADS["grouped"], "problems": n, "seed": GROUPED_SEED,
+                   "bytes_per_step": step_bytes, "buckets": ginfo["buckets"],
+                   "separate_members": ginfo["separate"], "tiles": ginfo["tiles"],
+                   "l2": "inputs larger than L2, no flush",
+                   "parallelism": f"replicas x{world}"},
+        "gbs": round(gbs, 3),
+        "loop": {"transposes_per_s": round(loop_value, 1), "ms_per_step": round(loop_ms, 4),
+                 "gbs": round(step_bytes / (loop_ms / 1e3) / 1e9, 3),
+                 "what": "librettExecute on every plan in turn (librett_c_execute_batch)"},
+        "speedup_vs_loop": round(loop_ms / ms, 3),
+        "untuned": {"ms_per_step": round(untuned_ms, 4),
+                    "transposes_per_s": round(world * n / (untuned_ms / 1e3), 1),
+                    "gbs": round(step_bytes / (untuned_ms / 1e3) / 1e9, 3)},
+        "tile_policy": {"per_size_class": policy, "tuned": tuned,
+                        "tune_s": None if tune_s is None else round(tune_s, 3),
+                        "classes": "<64KiB, <1MiB, <16MiB, larger",
+                        "values": "0 selector, 1 wide, 2 widest, 3 full-device model"},
+        "plan_s": round(plan_s, 3),
+        "group_create_s": round(create_s, 3),
+        "roofline": {"bound": "hbm", "kernel": "groupTileKernel", "achieved": round(gbs, 3),
+                     "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+                     "peak_source": peak_kind, "traffic": None,
+                     "basis": "algorithmic bytes of the whole group / graph time (the "
+                              "buckets run concurrently)"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,11 +660,14 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="suite")
-    ap.add_argument("--problems", type=int, default=200)
+    ap.add_argument("--problems", type=int, default=None,
+                    help="problems of the workload (suite: 200, grouped: 10000)")
     ap.add_argument("--cpu-budget", type=float, default=12.0,
                     help="seconds of host gather for the cpu_baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="grouped workload: keep the plan selector's tiles (no autotuning)")
     ap.add_argument("--dims", type=str, default=None, help="custom problem: comma-separated dims")
     ap.add_argument("--perm", type=str, default=None, help="custom problem: permutation")
     ap.add_argument("--es", type=int, default=8, help="custom problem: element bytes")
@@ -457,8 +681,12 @@ def main(argv=None):
         args.workload = "custom"
         args.custom = ([int(x) for x in args.dims.split(",")],
                        [int(x) for x in args.perm.split(",")], args.es)
+    if args.problems is None:
+        args.problems = 10000 if args.workload == "grouped" else 200
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "grouped":
+        return run_grouped(args)
     return run_engine(args)
 
 

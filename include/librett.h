@@ -91,6 +91,36 @@ librettResult librettDestroy(librettHandle handle);
  */
 librettResult librettExecute(librettHandle handle, void* idata, void* odata);
 
+/* ---- Grouped execution (no LibreTT counterpart) ----
+ * Many plans, each with its own input and output, executed as one CUDA
+ * graph: members are bucketed by kernel shape, each bucket is one launch over
+ * a device-resident descriptor table.  Creation plans, allocates (stream-
+ * ordered on `stream`), writes the tables and instantiates the graph
+ * (synchronising `stream` once); execution is one graph launch on `stream`;
+ * destruction frees in stream order.  The member plans may be destroyed once
+ * the group exists (the group keeps what it needs).  A member runs as a flat
+ * tile kernel inside its bucket; one whose pointers are not 16-byte aligned
+ * for its vector units, or whose problem needs more than eight grid ranks,
+ * runs its own plan's launch inside the same graph instead. */
+typedef unsigned int librettGroupHandle;
+
+librettResult librettGroupCreate(librettGroupHandle* group, int count, const librettHandle* plans,
+                                 void* const* idata, void* const* odata,
+                                 librett_gpuStream_t& stream);
+/* Autotunes the group's tile policy: times the policies per member size
+ * class on the group's own buffers (reads idata, overwrites odata), keeps the
+ * fastest and rebuilds the graph; synchronises the group's stream.  Later
+ * groups over the same batch signature (members' shapes, permutations,
+ * element sizes and 16-byte alignment) start from the tuned policy. */
+librettResult librettGroupTune(librettGroupHandle group);
+librettResult librettGroupExecute(librettGroupHandle group);
+librettResult librettGroupDestroy(librettGroupHandle group);
+
+/* One-shot: create a group on the first plan's stream, execute it once,
+ * destroy it.  Prefer a persistent group when the same batch repeats. */
+librettResult librettExecuteGrouped(int count, const librettHandle* plans, void* const* idata,
+                                    void* const* odata);
+
 #endif /* __cplusplus */
 
 #endif /* LIBRETT_H */

@@ -158,6 +158,36 @@ int librett_c_mlp_adam(float* params, const float* grads, float* m, float* v, in
  * inference librettPlan runs. */
 int librett_c_mlp_predict_host(const float* params, const float* x, int n, float* out);
 
+/* ---- Grouped execution (no LibreTT counterpart; see librett.h) ---- */
+#ifndef LIBRETT_H
+typedef unsigned int librettGroupHandle;
+#endif
+int librett_c_group_create(librettGroupHandle* group, int count, const librettHandle* plans,
+                           void* const* idata, void* const* odata, void* stream);
+/* As librett_c_group_create with the tile policy given per member size
+ * class (policy[4]: classes < 64 KiB, < 1 MiB, < 16 MiB, larger; values
+ * 0 = plan selector's tile, 1 = largest tile within 10% of the best sector
+ * efficiency, 2 = largest tile, 3 = analytic model for a full device). */
+int librett_c_group_create_policy(librettGroupHandle* group, int count,
+                                  const librettHandle* plans, void* const* idata,
+                                  void* const* odata, void* stream, const int* policy);
+int librett_c_group_tune(librettGroupHandle group);
+/* policy[4] in use, and whether it came from tuning (this group's or a
+ * cached one for the same batch signature). */
+int librett_c_group_policy(librettGroupHandle group, int* policy, int* tuned);
+int librett_c_group_execute(librettGroupHandle group);
+int librett_c_group_destroy(librettGroupHandle group);
+int librett_c_execute_grouped(int count, const librettHandle* plans, void* const* idata,
+                              void* const* odata);
+/* The plain per-tensor loop the grouped path replaces: librettExecute on
+ * each (plan, idata, odata) in order, one launch each; stops at and returns
+ * the first error. */
+int librett_c_execute_batch(int count, const librettHandle* plans, void* const* idata,
+                            void* const* odata);
+/* members, buckets (launches), members run separately, tiles, algorithmic bytes */
+int librett_c_group_info(librettGroupHandle group, int* members, int* buckets, int* separate,
+                         long long* tiles, long long* bytes);
+
 /* Number of device kernel launches this library issued since load (all
  * threads, all devices).  Used to count launches inside a timed region. */
 unsigned long long librett_c_launch_count(void);

@@ -123,6 +123,100 @@ def transpose_noalloc(dim, permutation, sizeofType: int, stream, idata: int, oda
                                                    _stream(stream), idata, odata)
 
 
+class Group:
+    """Owning wrapper of a group of plans executed as one CUDA graph
+    (librett_c_group_*; no LibreTT counterpart)."""
+
+    # tile policies per member size class (librett_c.h)
+    POLICY_SELECTOR, POLICY_WIDE, POLICY_WIDEST, POLICY_FILL = 0, 1, 2, 3
+
+    def __init__(self, plans, idata, odata, stream=None, *, policy=None):
+        n, hs, ins, outs = _handle_arrays(plans, idata, odata)
+        h = ctypes.c_uint(0)
+        lib = _lib.load()
+        if policy is None:
+            rc = lib.librett_c_group_create(ctypes.byref(h), n, hs, ins, outs, _stream(stream))
+        else:
+            pol = (ctypes.c_int * 4)(*[int(x) for x in policy])
+            rc = lib.librett_c_group_create_policy(ctypes.byref(h), n, hs, ins, outs,
+                                                   _stream(stream), pol)
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_group_create")
+        self.handle = h.value
+
+    def tune(self) -> None:
+        """librettGroupTune: time the tile policies on this group's buffers."""
+        rc = _lib.load().librett_c_group_tune(self.handle)
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_group_tune")
+
+    def policy(self) -> tuple[list[int], bool]:
+        pol = (ctypes.c_int * 4)()
+        tuned = ctypes.c_int(0)
+        rc = _lib.load().librett_c_group_policy(self.handle, pol, ctypes.byref(tuned))
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_group_policy")
+        return list(pol), bool(tuned.value)
+
+    def execute(self) -> None:
+        rc = _lib.load().librett_c_group_execute(self.handle)
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_group_execute")
+
+    def info(self) -> dict:
+        m, b, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        t, by = ctypes.c_longlong(), ctypes.c_longlong()
+        rc = _lib.load().librett_c_group_info(self.handle, ctypes.byref(m), ctypes.byref(b),
+                                              ctypes.byref(s), ctypes.byref(t), ctypes.byref(by))
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_group_info")
+        return {"members": m.value, "buckets": b.value, "separate": s.value, "tiles": t.value,
+                "bytes": by.value}
+
+    def destroy(self) -> None:
+        if self.handle is not None:
+            _lib.load().librett_c_group_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.destroy()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def _handle_arrays(plans, idata, odata):
+    n = len(plans)
+    if len(idata) != n or len(odata) != n:
+        raise ValueError("plans, idata and odata differ in length")
+    hs = (ctypes.c_uint * n)(*[p.handle if isinstance(p, Plan) else int(p) for p in plans])
+    ins = (ctypes.c_void_p * n)(*[int(x) for x in idata])
+    outs = (ctypes.c_void_p * n)(*[int(x) for x in odata])
+    return n, hs, ins, outs
+
+
+def execute_grouped(plans, idata, odata) -> None:
+    """librettExecuteGrouped: one-shot grouped execution on the first plan's stream."""
+    n, hs, ins, outs = _handle_arrays(plans, idata, odata)
+    rc = _lib.load().librett_c_execute_grouped(n, hs, ins, outs)
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_execute_grouped")
+
+
+def execute_batch(plans, idata, odata) -> None:
+    """The plain per-tensor loop: librettExecute on every plan in order."""
+    n, hs, ins, outs = _handle_arrays(plans, idata, odata)
+    rc = _lib.load().librett_c_execute_batch(n, hs, ins, outs)
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_execute_batch")
+
+
 def launch_count() -> int:
     return int(_lib.load().librett_c_launch_count())
 

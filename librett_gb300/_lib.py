@@ -110,6 +110,25 @@ C_FUNCTIONS = [
     ("librett_c_mlp_predict_host", ctypes.c_int,
      [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_int,
       ctypes.POINTER(ctypes.c_float)]),
+    ("librett_c_group_create", ctypes.c_int,
+     [ctypes.POINTER(_H), ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P),
+      ctypes.POINTER(_P), _P]),
+    ("librett_c_group_create_policy", ctypes.c_int,
+     [ctypes.POINTER(_H), ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P),
+      ctypes.POINTER(_P), _P, ctypes.POINTER(ctypes.c_int)]),
+    ("librett_c_group_tune", ctypes.c_int, [_H]),
+    ("librett_c_group_policy", ctypes.c_int,
+     [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    ("librett_c_group_execute", ctypes.c_int, [_H]),
+    ("librett_c_group_destroy", ctypes.c_int, [_H]),
+    ("librett_c_execute_grouped", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    ("librett_c_execute_batch", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    ("librett_c_group_info", ctypes.c_int,
+     [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
+      ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_launch_count", ctypes.c_ulonglong, []),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]
@@ -123,6 +142,10 @@ CXX_SYMBOLS = [
     "_Z14librettDestroyj",
     "_Z14librettExecutejPvS_",
 ]
+
+# C++ entry points with no LibreTT counterpart (grouped execution).
+CXX_GROUP_SYMBOLS = ["librettGroupCreate", "librettGroupTune", "librettGroupExecute",
+                     "librettGroupDestroy", "librettExecuteGrouped"]
 
 _lib = None
 

@@ -20,6 +20,7 @@
 #include "librett.h"
 #include "librett_c.h"
 #include "plan.h"
+#include "plans.h"
 #include "select.h"
 
 namespace lt {
@@ -28,23 +29,7 @@ extern std::atomic<unsigned long long> gLaunchCount;
 
 namespace {
 
-struct PlanObj {
-  lt::PlanDesc pd;
-  int selectedBy = 0;  // librett_plan_info.selected_by
-  cudaStream_t stream = nullptr;
-  int device = 0;
-  int numSMs = 0;
-  int lastGrid = 0;
-  void* tablesAlloc = nullptr;  // device tables of flat-pipeline plans
-  lt::DeviceTables tables;
-  PlanObj() = default;
-  PlanObj(const PlanObj&) = delete;
-  PlanObj& operator=(const PlanObj&) = delete;
-  // Stream-ordered release: launches already enqueued on the plan's stream
-  // finish before the tables are freed (LibreTT's plan destructor calls
-  // cudaFree, which synchronises the device, src/plan.cpp:1696-1703).
-  ~PlanObj() { lt::destroyDeviceTables(tablesAlloc, stream); }
-};
+using lt::PlanObj;
 
 // Plans are held by shared_ptr so that an execute that has looked a plan up
 // keeps it alive while a concurrent destroy removes it from the table.  The
@@ -61,7 +46,9 @@ struct DevInfo {
 std::mutex gDevMu;
 std::unordered_map<int, DevInfo> gDevs;
 
-bool currentDevice(int& dev, int& sms, std::string* name = nullptr) {
+}  // namespace
+
+bool lt::currentDevice(int& dev, int& sms, std::string* name) {
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   std::lock_guard<std::mutex> lk(gDevMu);
   auto it = gDevs.find(dev);
@@ -78,6 +65,10 @@ bool currentDevice(int& dev, int& sms, std::string* name = nullptr) {
   return true;
 }
 
+namespace {
+
+using lt::currentDevice;
+
 bool aligned(const void* p, size_t esize) {
   size_t a = esize < 16 ? esize : 16;
   return ((uintptr_t)p % a) == 0;
@@ -90,12 +81,22 @@ librettHandle storePlan(std::shared_ptr<PlanObj> obj) {
   return h;
 }
 
+}  // namespace
+
+namespace lt {
+
 std::shared_ptr<PlanObj> findPlan(librettHandle h) {
   std::shared_lock<std::shared_mutex> lk(gPlanMu);
   auto it = gPlans.find(h);
   if (it == gPlans.end()) return nullptr;
   return it->second;
 }
+
+}  // namespace lt
+
+namespace {
+
+using lt::findPlan;
 
 void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   std::memset(info, 0, sizeof(*info));

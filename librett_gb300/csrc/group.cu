@@ -1,0 +1,668 @@
+// Grouped execution (see group.h): member tile choice, bucketing, the CUDA
+// graph, the tile-policy autotuner, and the public librettGroup* /
+// librettExecuteGrouped entry points.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <unordered_map>
+#include <vector>
+
+#include "group.h"
+#include "kernels.cuh"
+#include "launch.h"
+#include "librett.h"
+#include "librett_c.h"
+#include "plans.h"
+#include "select.h"
+
+namespace lt {
+extern std::atomic<unsigned long long> gLaunchCount;
+namespace {
+
+// Writes every member's offset tables (same arithmetic as
+// writeTileTablesKernel); CTA b handles member b.
+__global__ void __launch_bounds__(256) writeGroupTablesKernel(const GroupTableJob* __restrict__ jobs) {
+  const GroupTableJob& jb = jobs[blockIdx.x];
+  const TileParams& p = jb.tp;
+  for (int u = threadIdx.x; u < p.nIn; u += blockDim.x) {
+    int rem = u * p.lv, off = 0;
+    for (int t = 0; t < p.nTR; ++t) {
+      const int e = p.trE[t];
+      const int q = rem / e;
+      off += (rem - q * e) * p.trSin[t];
+      rem = q;
+    }
+    jb.ldOff[u] = off;
+  }
+  for (int q = threadIdx.x; q < p.tileVol; q += blockDim.x) {
+    int rem = q, off = 0, jj = 0;
+    for (int i = 0; i < p.nTR; ++i) {
+      const int t = p.trOut[i];
+      const int e = p.trE[t];
+      const int d = rem / e;
+      const int c = rem - d * e;
+      rem = d;
+      off += c * p.trSout[t];
+      jj += c * p.trInTile[t];
+    }
+    jb.stSm[q] = (unsigned short)(jj + ((jj >> p.padShift) << p.padLog));
+    if (q % p.sv == 0) jb.stOff[q / p.sv] = off;
+  }
+}
+
+// Tile policies: how a member's flat tile is chosen from its candidates.
+enum GroupPolicy {
+  GP_SELECTOR = 0,  // the plan selector's choice for the tensor on its own
+  GP_WIDE = 1,      // the largest tile within 10% of the best sector efficiency
+  GP_WIDEST = 2,    // the largest tile
+  GP_FILL = 3,      // the analytic model with the device assumed full of other work
+  GP_COUNT = 4
+};
+
+// Member size classes (bytes of one tensor): < 64 KiB, < 1 MiB, < 16 MiB, larger.
+int sizeClass(long long bytes) {
+  return bytes < (1LL << 16) ? 0 : bytes < (1LL << 20) ? 1 : bytes < (1LL << 24) ? 2 : 3;
+}
+
+using Policy = std::array<int, GROUP_CLASSES>;
+
+struct Member {
+  std::shared_ptr<PlanObj> plan;  // the caller's plan (kept alive by the group)
+  const unsigned char* in;
+  unsigned char* out;
+  int cls;
+  bool aligned16;
+  int picked = -1;   // policy pd was chosen with (-1: none yet)
+  bool separate = false;  // runs its plan's own launch
+  PlanDesc pd;       // flat tile plan inside a bucket
+};
+
+struct Build {
+  void* alloc = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int buckets = 0, separate = 0;
+  long long tiles = 0;
+};
+
+void releaseBuild(Build& b, cudaStream_t s) {
+  // an executable graph still in flight is released when it completes
+  if (b.exec) cudaGraphExecDestroy(b.exec);
+  if (b.graph) cudaGraphDestroy(b.graph);
+  // stream-ordered: after every launch of this build on s
+  if (b.alloc) cudaFreeAsync(b.alloc, s);
+  b = Build();
+}
+
+struct GroupObj {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int numSMs = 0;
+  std::string devName;
+  std::vector<Member> members;
+  Policy policy{};
+  bool tuned = false;
+  uint64_t signature = 0;
+  long long bytes = 0;
+  Build built;
+  GroupObj() = default;
+  GroupObj(const GroupObj&) = delete;
+  GroupObj& operator=(const GroupObj&) = delete;
+  ~GroupObj() {
+    releaseBuild(built, stream);
+    // A separately launched member's plan frees its tables on the plan's own
+    // stream once the last reference goes: order that after this group.
+    cudaEvent_t done = nullptr;
+    for (const Member& m : members) {
+      if (!m.separate || m.plan->stream == stream) continue;
+      if (done == nullptr && cudaEventCreateWithFlags(&done, cudaEventDisableTiming) == cudaSuccess)
+        cudaEventRecord(done, stream);
+      if (done) cudaStreamWaitEvent(m.plan->stream, done, 0);
+    }
+    if (done) cudaEventDestroy(done);
+  }
+};
+
+std::mutex gGroupMu;
+std::unordered_map<librettGroupHandle, std::shared_ptr<GroupObj>> gGroups;
+std::atomic<librettGroupHandle> gNextGroup{0};
+
+// Tuned policies by batch signature (members' shapes, alignment, device).
+std::mutex gTuneMu;
+std::unordered_map<uint64_t, Policy> gTuneCache;
+
+size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+uint64_t fnv(uint64_t h, uint64_t v) {
+  for (int i = 0; i < 8; ++i) {
+    h ^= (v >> (8 * i)) & 0xff;
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, const GroupTensor* tens,
+                              const int* map, uint32_t tiles, int smem, cudaStream_t s) {
+  switch (es) {
+    case 4: return launchGroupTile4(lv, sv, nl, tens, map, tiles, smem, s);
+    case 8: return launchGroupTile8(lv, sv, nl, tens, map, tiles, smem, s);
+    case 16: return launchGroupTile16(lv, sv, nl, tens, map, tiles, smem, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// Flat tile plan of member m under a policy; false when the member must run
+// its plan's own launch.
+bool pickTile(const Member& m, int policy, int sms, const std::string& dev, PlanDesc& out) {
+  const PlanDesc& own = m.plan->pd;
+  if (policy == GP_SELECTOR && own.kernel == K_TILE && own.pipe == PIPE_FLAT) {
+    out = own;
+  } else {
+    std::vector<PlanDesc> c = flatTileCandidates(own.f, policy == GP_FILL ? sms * 64 : sms);
+    if (c.empty()) return false;
+    int k = 0;
+    auto eff = [](const PlanDesc& p) { return std::min(p.effIn, p.effOut); };
+    switch (policy) {
+      case GP_SELECTOR:
+        k = choosePlan(c, sms, dev.c_str(), nullptr);
+        break;
+      case GP_FILL:
+        k = chooseHeuristic(c);
+        break;
+      case GP_WIDE: {
+        double best = 0.0;
+        for (const PlanDesc& p : c) best = std::max(best, eff(p));
+        k = -1;
+        for (int i = 0; i < (int)c.size(); ++i) {
+          if (eff(c[i]) < 0.9 * best) continue;
+          if (k < 0 || c[i].tile.tileVol > c[k].tile.tileVol ||
+              (c[i].tile.tileVol == c[k].tile.tileVol && c[i].cost < c[k].cost))
+            k = i;
+        }
+        break;
+      }
+      default:  // GP_WIDEST
+        for (int i = 1; i < (int)c.size(); ++i)
+          if (c[i].tile.tileVol > c[k].tile.tileVol ||
+              (c[i].tile.tileVol == c[k].tile.tileVol && eff(c[i]) > eff(c[k])))
+            k = i;
+        break;
+    }
+    out = c[k];
+  }
+  if (!m.aligned16 && (out.tile.lv > 1 || out.tile.sv > 1)) {
+    // pointers not 16-byte aligned: the same tile in element units
+    if (!finalizePlan(out)) return false;
+    out.tile = out.tileScalar;
+    out.slots = out.slotsScalar;
+    out.smemBytes = out.tile.smStride * out.f.esize;
+  }
+  return out.tile.nGR <= GROUP_MAXG;
+}
+
+struct Bucket {
+  int es, lv, sv, nl;
+  int smem = 0;
+  uint32_t tiles = 0;
+  long long bytes = 0;
+  std::vector<int> members;  // indices into GroupObj::members
+  size_t tensOff = 0, mapOff = 0;
+};
+
+// (Re)builds the device image and the graph for a policy.  Synchronises the
+// group's stream.
+librettResult build(GroupObj& g, const Policy& pol) {
+  for (Member& m : g.members) {
+    const int p = pol[m.cls];
+    if (m.picked == p) continue;
+    m.separate = !pickTile(m, p, g.numSMs, g.devName, m.pd);
+    m.picked = p;
+  }
+  if (cudaStreamSynchronize(g.stream) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  releaseBuild(g.built, g.stream);
+  g.policy = pol;
+  Build& B = g.built;
+
+  // buckets by kernel shape
+  std::map<std::tuple<int, int, int, int>, int> key2b;
+  std::vector<Bucket> buckets;
+  for (int i = 0; i < (int)g.members.size(); ++i) {
+    const Member& m = g.members[i];
+    if (m.separate) {
+      ++B.separate;
+      continue;
+    }
+    const PlanDesc& pd = m.pd;
+    auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots);
+    auto it = key2b.find(key);
+    if (it == key2b.end()) {
+      Bucket b;
+      b.es = pd.f.esize;
+      b.lv = pd.tile.lv;
+      b.sv = pd.tile.sv;
+      b.nl = pd.slots;
+      it = key2b.emplace(key, (int)buckets.size()).first;
+      buckets.push_back(b);
+    }
+    Bucket& b = buckets[it->second];
+    b.members.push_back(i);
+    if ((uint64_t)b.tiles + pd.tile.numTiles >= (uint64_t(1) << 31)) return LIBRETT_INVALID_PARAMETER;
+    b.tiles += pd.tile.numTiles;
+    b.bytes += 2 * pd.f.vol * (long long)pd.f.esize;
+    b.smem = std::max(b.smem, pd.smemBytes);
+  }
+  B.buckets = (int)buckets.size();
+
+  // one allocation: descriptors, tile maps, table jobs (written from the
+  // host), then the members' offset tables (written by a kernel)
+  size_t off = 0;
+  for (Bucket& b : buckets) {
+    b.tensOff = off;
+    off = align16(off + b.members.size() * sizeof(GroupTensor));
+  }
+  for (Bucket& b : buckets) {
+    b.mapOff = off;
+    off = align16(off + (size_t)b.tiles * sizeof(int));
+    B.tiles += b.tiles;
+  }
+  std::vector<int> jobOf(g.members.size(), -1);
+  int nJobs = 0;
+  for (const Bucket& b : buckets)
+    for (int i : b.members) jobOf[i] = nJobs++;
+  const size_t jobsOff = off;
+  off = align16(off + (size_t)nJobs * sizeof(GroupTableJob));
+  const size_t imageBytes = off;
+  std::vector<size_t> tabOff(g.members.size(), 0);
+  for (const Bucket& b : buckets)
+    for (int i : b.members) {
+      size_t so, smo;
+      tabOff[i] = off;
+      off = align16(off + deviceTableBytes(g.members[i].pd.tile, &so, &smo));
+    }
+  const size_t total = std::max<size_t>(off, 16);
+  if (cudaMallocAsync(&B.alloc, total, g.stream) != cudaSuccess) {
+    B.alloc = nullptr;
+    return LIBRETT_INTERNAL_ERROR;
+  }
+  unsigned char* base = static_cast<unsigned char*>(B.alloc);
+  std::vector<unsigned char> host(std::max<size_t>(imageBytes, 16), 0);
+  GroupTableJob* jobs = reinterpret_cast<GroupTableJob*>(host.data() + jobsOff);
+  for (Bucket& b : buckets) {
+    GroupTensor* tens = reinterpret_cast<GroupTensor*>(host.data() + b.tensOff);
+    int* map = reinterpret_cast<int*>(host.data() + b.mapOff);
+    uint32_t first = 0;
+    for (size_t k = 0; k < b.members.size(); ++k) {
+      const int i = b.members[k];
+      const Member& m = g.members[i];
+      const TileParams& tp = m.pd.tile;
+      size_t so, smo;
+      deviceTableBytes(tp, &so, &smo);
+      unsigned char* tb = base + tabOff[i];
+      GroupTensor& t = tens[k];
+      std::memset(&t, 0, sizeof(t));
+      t.in = m.in;
+      t.out = m.out;
+      t.ldOff = reinterpret_cast<const int*>(tb);
+      t.stOff = reinterpret_cast<const int*>(tb + so);
+      t.stSm = reinterpret_cast<const unsigned short*>(tb + smo);
+      t.firstTile = first;
+      t.nIn = tp.nIn;
+      t.nOut = tp.nOut;
+      t.padShift = tp.padShift;
+      t.padLog = tp.padLog;
+      t.nGR = tp.nGR;
+      for (int q = 0; q < tp.nGR; ++q) {
+        t.grDiv[q] = tp.grDiv[q];
+        t.grSin[q] = tp.grSin[q];
+        t.grSout[q] = tp.grSout[q];
+        t.grLastIn[q] = tp.grLastIn[q];
+        t.grLastOut[q] = tp.grLastOut[q];
+      }
+      for (uint32_t x = 0; x < tp.numTiles; ++x) map[first + x] = (int)k;
+      first += tp.numTiles;
+      GroupTableJob jb;
+      std::memset(&jb, 0, sizeof(jb));
+      jb.tp = tp;
+      jb.ldOff = reinterpret_cast<int*>(tb);
+      jb.stOff = reinterpret_cast<int*>(tb + so);
+      jb.stSm = reinterpret_cast<unsigned short*>(tb + smo);
+      std::memcpy(jobs + jobOf[i], &jb, sizeof(jb));
+    }
+  }
+  // (a pageable source is consumed before cudaMemcpyAsync returns)
+  cudaError_t err = cudaMemcpyAsync(base, host.data(), imageBytes, cudaMemcpyHostToDevice, g.stream);
+  if (err == cudaSuccess && nJobs > 0)
+    writeGroupTablesKernel<<<(unsigned)nJobs, 256, 0, g.stream>>>(
+        reinterpret_cast<const GroupTableJob*>(base + jobsOff));
+  if (err == cudaSuccess) err = cudaGetLastError();
+  // a separately launched member's tables were written on its plan's stream
+  for (const Member& m : g.members)
+    if (err == cudaSuccess && m.separate && m.plan->stream != g.stream)
+      err = cudaStreamSynchronize(m.plan->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(g.stream);
+  if (err != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+
+  // The graph: one node per bucket plus one per separate member, spread over
+  // parallel branches, largest work first onto the least-loaded branch.
+  struct Node {
+    long long bytes;
+    int bucket;  // >= 0: bucket index; < 0: separate member -bucket-1
+  };
+  std::vector<Node> nodes;
+  for (int b = 0; b < (int)buckets.size(); ++b) nodes.push_back({buckets[b].bytes, b});
+  for (int i = 0; i < (int)g.members.size(); ++i)
+    if (g.members[i].separate)
+      nodes.push_back({2 * g.members[i].pd.f.vol * (long long)g.members[i].pd.f.esize, -i - 1});
+  std::stable_sort(nodes.begin(), nodes.end(),
+                   [](const Node& a, const Node& b) { return a.bytes > b.bytes; });
+  const int branches = std::max(1, std::min((int)nodes.size(), 8));
+  std::vector<long long> load(branches, 0);
+  cudaStream_t cap = nullptr;
+  std::vector<cudaStream_t> side(branches, nullptr);
+  std::vector<cudaEvent_t> ev(branches + 1, nullptr);
+  bool ok = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess;
+  for (int b = 0; ok && b < branches; ++b)
+    ok = cudaStreamCreateWithFlags(&side[b], cudaStreamNonBlocking) == cudaSuccess;
+  for (int b = 0; ok && b <= branches; ++b)
+    ok = cudaEventCreateWithFlags(&ev[b], cudaEventDisableTiming) == cudaSuccess;
+  if (ok) ok = cudaStreamBeginCapture(cap, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+  if (ok) {
+    bool launched = cudaEventRecord(ev[branches], cap) == cudaSuccess;
+    for (int b = 0; launched && b < branches; ++b)
+      launched = cudaStreamWaitEvent(side[b], ev[branches], 0) == cudaSuccess;
+    for (const Node& nd : nodes) {
+      if (!launched) break;
+      const int br = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      load[br] += nd.bytes;
+      if (nd.bucket >= 0) {
+        const Bucket& b = buckets[nd.bucket];
+        launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl,
+                                     reinterpret_cast<const GroupTensor*>(base + b.tensOff),
+                                     reinterpret_cast<const int*>(base + b.mapOff), b.tiles,
+                                     b.smem, side[br]) == cudaSuccess;
+      } else {
+        const Member& m = g.members[-nd.bucket - 1];
+        int grid = 0;
+        launched = launchPlan(m.plan->pd, &m.plan->tables, m.in, m.out, side[br], g.numSMs,
+                              &grid) == cudaSuccess;
+      }
+    }
+    for (int b = 0; b < branches; ++b) {
+      cudaEventRecord(ev[b], side[b]);
+      cudaStreamWaitEvent(cap, ev[b], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const bool ended = cudaStreamEndCapture(cap, &graph) == cudaSuccess;
+    ok = launched && ended && graph != nullptr;
+    B.graph = graph;
+    if (ok) ok = cudaGraphInstantiate(&B.exec, graph, 0) == cudaSuccess;
+  }
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t s : side)
+    if (s) cudaStreamDestroy(s);
+  if (cap) cudaStreamDestroy(cap);
+  if (!ok) {
+    cudaGetLastError();
+    return LIBRETT_INTERNAL_ERROR;
+  }
+  return LIBRETT_SUCCESS;
+}
+
+uint64_t batchSignature(const GroupObj& g) {
+  uint64_t h = 1469598103934665603ULL;
+  h = fnv(h, (uint64_t)g.numSMs);
+  h = fnv(h, g.members.size());
+  for (const Member& m : g.members) {
+    const Fused& f = m.plan->pd.f;
+    h = fnv(h, ((uint64_t)f.rank << 8) | ((uint64_t)f.esize << 1) | (m.aligned16 ? 1 : 0));
+    for (int r = 0; r < f.rank; ++r) h = fnv(h, ((uint64_t)f.dim[r] << 5) | (uint64_t)f.perm[r]);
+  }
+  return h;
+}
+
+librettResult create(librettGroupHandle* handle, int count, const librettHandle* plans,
+                     void* const* idata, void* const* odata, cudaStream_t stream,
+                     const int* policy) {
+  if (handle == nullptr || count < 1 || plans == nullptr || idata == nullptr || odata == nullptr)
+    return LIBRETT_INVALID_PARAMETER;
+  if (policy != nullptr)
+    for (int c = 0; c < GROUP_CLASSES; ++c)
+      if (policy[c] < 0 || policy[c] >= GP_COUNT) return LIBRETT_INVALID_PARAMETER;
+  int dev = 0, sms = 0;
+  auto g = std::make_shared<GroupObj>();
+  if (!currentDevice(dev, sms, &g->devName)) return LIBRETT_INTERNAL_ERROR;
+  g->stream = stream;
+  g->device = dev;
+  g->numSMs = sms;
+  g->members.resize(count);
+  for (int i = 0; i < count; ++i) {
+    Member& m = g->members[i];
+    m.plan = findPlan(plans[i]);
+    if (!m.plan) return LIBRETT_INVALID_PLAN;
+    if (m.plan->device != dev) return LIBRETT_INVALID_DEVICE;
+    m.in = static_cast<const unsigned char*>(idata[i]);
+    m.out = static_cast<unsigned char*>(odata[i]);
+    const Fused& f = m.plan->pd.f;
+    const uintptr_t a = f.esize < 16 ? f.esize : 16;
+    if (m.in == nullptr || m.out == nullptr || (const void*)m.in == (const void*)m.out ||
+        (uintptr_t)m.in % a || (uintptr_t)m.out % a)
+      return LIBRETT_INVALID_PARAMETER;
+    const long long bytes = f.vol * (long long)f.esize;
+    g->bytes += 2 * bytes;
+    m.cls = sizeClass(bytes);
+    m.aligned16 = (uintptr_t)m.in % 16 == 0 && (uintptr_t)m.out % 16 == 0;
+  }
+  g->signature = batchSignature(*g);
+  Policy pol;
+  pol.fill(GP_SELECTOR);
+  if (policy != nullptr) {
+    std::copy(policy, policy + GROUP_CLASSES, pol.begin());
+  } else {
+    std::lock_guard<std::mutex> lk(gTuneMu);
+    auto it = gTuneCache.find(g->signature);
+    if (it != gTuneCache.end()) {
+      pol = it->second;
+      g->tuned = true;
+    }
+  }
+  librettResult r = build(*g, pol);
+  if (r != LIBRETT_SUCCESS) return r;
+  librettGroupHandle h = gNextGroup.fetch_add(1);
+  {
+    std::lock_guard<std::mutex> lk(gGroupMu);
+    gGroups[h] = g;
+  }
+  *handle = h;
+  return LIBRETT_SUCCESS;
+}
+
+std::shared_ptr<GroupObj> findGroup(librettGroupHandle h) {
+  std::lock_guard<std::mutex> lk(gGroupMu);
+  auto it = gGroups.find(h);
+  return it == gGroups.end() ? nullptr : it->second;
+}
+
+librettResult launch(GroupObj& g) {
+  if (g.built.exec == nullptr || cudaGraphLaunch(g.built.exec, g.stream) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
+  gLaunchCount.fetch_add((unsigned long long)g.built.buckets + g.built.separate,
+                         std::memory_order_relaxed);
+  return LIBRETT_SUCCESS;
+}
+
+librettResult execute(librettGroupHandle h) {
+  std::shared_ptr<GroupObj> g = findGroup(h);
+  if (!g) return LIBRETT_INVALID_PLAN;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  if (dev != g->device) return LIBRETT_INVALID_DEVICE;
+  return launch(*g);
+}
+
+// Best of three timed executions after one untimed one (milliseconds).
+bool timeBuild(GroupObj& g, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
+  if (launch(g) != LIBRETT_SUCCESS) return false;
+  float best = -1.f;
+  for (int rep = 0; rep < 3; ++rep) {
+    if (cudaEventRecord(e0, g.stream) != cudaSuccess || launch(g) != LIBRETT_SUCCESS ||
+        cudaEventRecord(e1, g.stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+      return false;
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) return false;
+    if (best < 0.f || t < best) best = t;
+  }
+  *ms = best;
+  return true;
+}
+
+// Coordinate descent over the size classes (largest first): each class
+// tries every policy with the others fixed and keeps one that is at least 2%
+// faster.  Times on the group's own buffers (reads the inputs, overwrites
+// the outputs); the result is cached by batch signature.
+librettResult tune(librettGroupHandle h) {
+  std::shared_ptr<GroupObj> gp = findGroup(h);
+  if (!gp) return LIBRETT_INVALID_PLAN;
+  GroupObj& g = *gp;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  if (dev != g.device) return LIBRETT_INVALID_DEVICE;
+  bool present[GROUP_CLASSES] = {};
+  for (const Member& m : g.members) present[m.cls] = true;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    return LIBRETT_INTERNAL_ERROR;
+  }
+  librettResult r = LIBRETT_SUCCESS;
+  Policy cur = g.policy;
+  float best = 0.f;
+  if (!timeBuild(g, e0, e1, &best)) r = LIBRETT_INTERNAL_ERROR;
+  for (int c = GROUP_CLASSES - 1; c >= 0 && r == LIBRETT_SUCCESS; --c) {
+    if (!present[c]) continue;
+    for (int p = 0; p < GP_COUNT && r == LIBRETT_SUCCESS; ++p) {
+      if (p == cur[c]) continue;
+      Policy trial = cur;
+      trial[c] = p;
+      float t = 0.f;
+      r = build(g, trial);
+      if (r == LIBRETT_SUCCESS && !timeBuild(g, e0, e1, &t)) r = LIBRETT_INTERNAL_ERROR;
+      if (r == LIBRETT_SUCCESS && t < 0.98f * best) {
+        best = t;
+        cur = trial;
+      }
+    }
+  }
+  if (r == LIBRETT_SUCCESS && g.policy != cur) r = build(g, cur);
+  if (r != LIBRETT_SUCCESS && build(g, cur) != LIBRETT_SUCCESS) g.built = Build();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (r != LIBRETT_SUCCESS) return r;
+  g.tuned = true;
+  std::lock_guard<std::mutex> lk(gTuneMu);
+  gTuneCache[g.signature] = cur;
+  return LIBRETT_SUCCESS;
+}
+
+librettResult destroy(librettGroupHandle h) {
+  std::lock_guard<std::mutex> lk(gGroupMu);
+  auto it = gGroups.find(h);
+  if (it == gGroups.end()) return LIBRETT_INVALID_PLAN;
+  gGroups.erase(it);
+  return LIBRETT_SUCCESS;
+}
+
+}  // namespace
+}  // namespace lt
+
+librettResult librettGroupCreate(librettGroupHandle* group, int count, const librettHandle* plans,
+                                 void* const* idata, void* const* odata,
+                                 librett_gpuStream_t& stream) {
+  return lt::create(group, count, plans, idata, odata, stream, nullptr);
+}
+
+librettResult librettGroupTune(librettGroupHandle group) { return lt::tune(group); }
+
+librettResult librettGroupExecute(librettGroupHandle group) { return lt::execute(group); }
+
+librettResult librettGroupDestroy(librettGroupHandle group) { return lt::destroy(group); }
+
+librettResult librettExecuteGrouped(int count, const librettHandle* plans, void* const* idata,
+                                    void* const* odata) {
+  if (count < 1 || plans == nullptr) return LIBRETT_INVALID_PARAMETER;
+  std::shared_ptr<lt::PlanObj> first = lt::findPlan(plans[0]);
+  if (!first) return LIBRETT_INVALID_PLAN;
+  librettGroupHandle g = 0;
+  librettResult r = lt::create(&g, count, plans, idata, odata, first->stream, nullptr);
+  if (r != LIBRETT_SUCCESS) return r;
+  r = lt::execute(g);
+  lt::destroy(g);
+  return r;
+}
+
+extern "C" {
+
+int librett_c_group_create(librettGroupHandle* group, int count, const librettHandle* plans,
+                           void* const* idata, void* const* odata, void* stream) {
+  return lt::create(group, count, plans, idata, odata, (cudaStream_t)stream, nullptr);
+}
+
+int librett_c_group_create_policy(librettGroupHandle* group, int count,
+                                  const librettHandle* plans, void* const* idata,
+                                  void* const* odata, void* stream, const int* policy) {
+  if (policy == nullptr) return LIBRETT_INVALID_PARAMETER;
+  return lt::create(group, count, plans, idata, odata, (cudaStream_t)stream, policy);
+}
+
+int librett_c_group_tune(librettGroupHandle group) { return librettGroupTune(group); }
+
+int librett_c_group_execute(librettGroupHandle group) { return librettGroupExecute(group); }
+
+int librett_c_group_destroy(librettGroupHandle group) { return librettGroupDestroy(group); }
+
+int librett_c_execute_grouped(int count, const librettHandle* plans, void* const* idata,
+                              void* const* odata) {
+  return librettExecuteGrouped(count, plans, idata, odata);
+}
+
+int librett_c_execute_batch(int count, const librettHandle* plans, void* const* idata,
+                            void* const* odata) {
+  if (count < 0 || (count > 0 && (plans == nullptr || idata == nullptr || odata == nullptr)))
+    return LIBRETT_INVALID_PARAMETER;
+  for (int i = 0; i < count; ++i) {
+    const librettResult r = librettExecute(plans[i], idata[i], odata[i]);
+    if (r != LIBRETT_SUCCESS) return r;
+  }
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_group_info(librettGroupHandle group, int* members, int* buckets, int* separate,
+                         long long* tiles, long long* bytes) {
+  std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
+  if (!g) return LIBRETT_INVALID_PLAN;
+  if (members) *members = (int)g->members.size();
+  if (buckets) *buckets = g->built.buckets;
+  if (separate) *separate = g->built.separate;
+  if (tiles) *tiles = g->built.tiles;
+  if (bytes) *bytes = g->bytes;
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_group_policy(librettGroupHandle group, int* policy, int* tuned) {
+  std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
+  if (!g) return LIBRETT_INVALID_PLAN;
+  if (policy)
+    for (int c = 0; c < lt::GROUP_CLASSES; ++c) policy[c] = g->policy[c];
+  if (tuned) *tuned = g->tuned ? 1 : 0;
+  return LIBRETT_SUCCESS;
+}
+
+}  // extern "C"

@@ -2,4 +2,5 @@
 #include "tile_kernel.cuh"
 #define LT_ES 4
 #define LT_LAUNCH_NAME launchTile4
+#define LT_GROUP_NAME launchGroupTile4
 #include "tile_launch.inc"

@@ -2,4 +2,5 @@
 #include "tile_kernel.cuh"
 #define LT_ES 8
 #define LT_LAUNCH_NAME launchTile8
+#define LT_GROUP_NAME launchGroupTile8
 #include "tile_launch.inc"

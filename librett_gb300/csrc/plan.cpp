@@ -250,23 +250,21 @@ namespace {
 // Wavefronts of 32-lane accesses: phases of 128 bytes; per phase the largest
 // number of distinct 4-byte words any bank is asked for (a lane touches
 // wordsPerLane consecutive words, so it never hits one bank twice).
+// Addresses within one access are distinct (every lane touches its own
+// elements, and the padding map is injective), so a phase costs the largest
+// number of words that fall into one bank.
 long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
   long long cost = 0;
   const int lanesPerPhase = std::max(1, 32 / wordsPerLane);
   for (int ph = 0; ph < 32; ph += lanesPerPhase) {
-    int words[32][4];
-    int cnt[32] = {};
+    unsigned char cnt[32] = {};
     int maxPerBank = 0;
     for (int l = ph; l < ph + lanesPerPhase; ++l) {
       if (!act[l]) continue;
       for (int q = 0; q < wordsPerLane; ++q) {
-        const int wa = addr[l] + q, bk = wa & 31;
-        bool dup = false;
-        for (int k = 0; k < cnt[bk] && k < 4; ++k)
-          if (words[bk][k] == wa) { dup = true; break; }
-        if (dup) continue;
-        if (cnt[bk] < 4) words[bk][cnt[bk]] = wa;
-        if (++cnt[bk] > maxPerBank) maxPerBank = cnt[bk];
+        const int bk = (addr[l] + q) & 31;
+        const int c = ++cnt[bk];
+        maxPerBank = c > maxPerBank ? c : maxPerBank;
       }
     }
     cost += maxPerBank;
@@ -676,6 +674,50 @@ void modelRows(PlanDesc& pd, int numSMs) {
 
 }  // namespace
 
+// Tile candidates: (target contiguous run bytes, maximum tile bytes,
+// minimum tile bytes), each in the flat pipeline and, unless flatOnly, the
+// two persistent pipelines.
+void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out) {
+  const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
+                          {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
+                          {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
+  std::vector<std::vector<int64_t>> seen;
+  const int V = 16 / f.esize;
+  for (auto& kb : knobs) {
+    int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
+    int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
+    int64_t fillVol = std::min<int64_t>(maxVol, kb[2] / f.esize);
+    int64_t e[MAXR];
+    chooseExtents(f, target, maxVol, fillVol, e);
+    std::vector<int64_t> key(e, e + f.rank);
+    if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+    seen.push_back(key);
+    TileParams geom;
+    if (!buildTileGeometry(f, e, V, V, geom)) continue;
+    for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
+      if (pipe != PIPE_FLAT && flatOnly) continue;
+      PlanDesc pd;
+      pd.f = f;
+      pd.targetRunBytes = kb[0];
+      pd.maxTileBytes = kb[1];
+      if (!buildTile(f, e, pipe, geom, pd)) continue;
+      modelTile(pd, numSMs);
+      out.push_back(pd);
+    }
+  }
+}
+
+std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs) {
+  std::vector<PlanDesc> out;
+  out.reserve(12);
+  appendTileCandidates(f, numSMs < 1 ? 1 : numSMs, true, out);
+  for (size_t i = 0; i < out.size(); ++i) {
+    out[i].candidate = (int)i;
+    out[i].numCandidates = (int)out.size();
+  }
+  return out;
+}
+
 namespace {
 std::atomic<int> gAllPipelines{-1};
 }
@@ -694,6 +736,7 @@ bool allPipelines() {
 
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
   std::vector<PlanDesc> out;
+  out.reserve(allPipelines() ? 32 : 12);
   if (numSMs < 1) numSMs = 1;
   if (f.rank == 1) {
     PlanDesc pd;
@@ -727,36 +770,7 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
         out.push_back(pd);
       }
     }
-    // Tile candidates: (target contiguous run bytes, maximum tile bytes,
-    // minimum tile bytes), each in the three pipelines.
-    const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
-                            {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
-                            {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
-    std::vector<std::vector<int64_t>> seen;
-    const int V = 16 / f.esize;
-    for (auto& kb : knobs) {
-      int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
-      int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
-      int64_t fillVol = std::min<int64_t>(maxVol, kb[2] / f.esize);
-      int64_t e[MAXR];
-      chooseExtents(f, target, maxVol, fillVol, e);
-      std::vector<int64_t> key(e, e + f.rank);
-      if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
-      seen.push_back(key);
-      TileParams geom;
-      if (!buildTileGeometry(f, e, V, V, geom)) continue;
-      const bool all = allPipelines();
-      for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
-        if (pipe != PIPE_FLAT && !all) continue;
-        PlanDesc pd;
-        pd.f = f;
-        pd.targetRunBytes = kb[0];
-        pd.maxTileBytes = kb[1];
-        if (!buildTile(f, e, pipe, geom, pd)) continue;
-        modelTile(pd, numSMs);
-        out.push_back(pd);
-      }
-    }
+    appendTileCandidates(f, numSMs, !allPipelines(), out);
   }
   for (size_t i = 0; i < out.size(); ++i) {
     out[i].candidate = (int)i;

@@ -171,6 +171,12 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
 void setAllPipelines(bool all);
 bool allPipelines();
 
+// Tile candidates in the one-tile-per-CTA pipeline only, for any fused
+// problem (a fused rank-1 copy becomes a one-rank tile); used where every
+// member of a batch must run in that pipeline (grouped execution).
+std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs);
+void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out);
+
 // Index of the candidate the analytic model prefers.
 int chooseHeuristic(const std::vector<PlanDesc>& cands);
 

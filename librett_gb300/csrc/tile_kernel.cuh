@@ -19,6 +19,7 @@
 // and only two 64-bit bases change per tile.
 #pragma once
 
+#include "group.h"
 #include "kernels.cuh"
 
 namespace lt {
@@ -287,6 +288,80 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   }
   __syncthreads();
   storeTile<ES, SV>(p, stOff, stSm, s, out + bout);
+}
+
+// Grouped flat kernel: CTA b moves one tile of tensor tileTensor[b] of a
+// bucket; the tensor's descriptor gives its pointers, offset tables and the
+// decode of its local tile index (same arithmetic as decodeTile).
+template <int ES, int LV, int SV, int NL>
+__global__ void __launch_bounds__(TILE_THREADS)
+groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ tileTensor) {
+  using T = typename Word<ES>::T;
+  using LT = typename Word<ES * LV>::T;
+  using ST = typename Word<ES * SV>::T;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* s = reinterpret_cast<T*>(smraw);
+  const GroupTensor* g = tens + __ldg(tileTensor + blockIdx.x);
+  uint32_t rem = blockIdx.x - g->firstTile;
+  long long bin = 0, bout = 0;
+  const int nGR = g->nGR;
+  // unrolled with a predicate so that the descriptor loads issue together
+#pragma unroll
+  for (int k = 0; k < GROUP_MAXG; ++k) {
+    if (k < nGR) {
+      const FastDiv dv = g->grDiv[k];
+      const uint32_t q = fdiv(rem, dv);
+      const uint32_t c = rem - q * dv.d;
+      rem = q;
+      const bool last = c + 1 == dv.d;
+      bin += last ? g->grLastIn[k] : (long long)c * g->grSin[k];
+      bout += last ? g->grLastOut[k] : (long long)c * g->grSout[k];
+    }
+  }
+  const T* in = reinterpret_cast<const T*>(g->in) + bin;
+  T* out = reinterpret_cast<T*>(g->out) + bout;
+  const int* ldOff = g->ldOff;
+  const int nIn = g->nIn, nOut = g->nOut, padShift = g->padShift, padLog = g->padLog;
+  LT v[NL];
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    const int u = threadIdx.x + k * TILE_THREADS;
+    if (u < nIn) v[k] = *reinterpret_cast<const LT*>(in + __ldg(ldOff + u));
+  }
+#pragma unroll
+  for (int k = 0; k < NL; ++k) {
+    const int u = threadIdx.x + k * TILE_THREADS;
+    if (u < nIn) {
+      const int j = u * LV;
+      *reinterpret_cast<LT*>(s + j + ((j >> padShift) << padLog)) = v[k];
+    }
+  }
+  __syncthreads();
+  const int* stOff = g->stOff;
+  const unsigned short* stSm = g->stSm;
+#pragma unroll 4
+  for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
+    T* dst = out + __ldg(stOff + w);
+    if constexpr (SV == 1) {
+      *dst = s[__ldg(stSm + w)];
+    } else {
+      T e[SV];
+      if constexpr (SV == 2) {
+        const unsigned idx = __ldg(reinterpret_cast<const unsigned*>(stSm + 2 * w));
+        e[0] = s[idx & 0xffffu];
+        e[1] = s[idx >> 16];
+      } else {
+        const uint2 idx = __ldg(reinterpret_cast<const uint2*>(stSm + 4 * w));
+        e[0] = s[idx.x & 0xffffu];
+        e[1] = s[idx.x >> 16];
+        e[2] = s[idx.y & 0xffffu];
+        e[3] = s[idx.y >> 16];
+      }
+      ST val;
+      __builtin_memcpy(&val, e, sizeof(ST));
+      *reinterpret_cast<ST*>(dst) = val;
+    }
+  }
 }
 
 }  // namespace lt

@@ -3,7 +3,7 @@
 // Links against the LibreTT library compiled unmodified from its sources by
 // oracle/ref_bench/run_ref.py, and calls it only through its public API
 // (librettPlan / librettPlanMeasure / librettExecute / librettDestroy,
-// LibreTT src/librett.h:57-121).  Two modes:
+// LibreTT src/librett.h:57-121).  Three modes:
 //
 //   ref_driver golden <cases> <outdir>
 //       for each case, fill the input (LibreTT's test conventions: element i
@@ -12,7 +12,11 @@
 //   ref_driver bench <cases> <steps> <warmup> <measure:0|1>
 //       for each case, plan (librettPlan, or librettPlanMeasure when
 //       measure=1), then time <steps> executes after <warmup> untimed ones
-//       with CUDA events on the plan's stream; print one JSON line per case.
+//       with CUDA events on the plan's stream; print one JSON line per case;
+//   ref_driver loop <cases> <steps> <warmup>
+//       plan every case, then time the per-tensor loop (librettExecute on
+//       every case in turn, each tensor at its own offset of one buffer);
+//       print one JSON line.
 //
 // Case file: one case per line, "rank d0 .. d{r-1} p0 .. p{r-1} es kind"
 // (kind 0 = value pattern, 1 = word pattern, 2 = leave memory as is).
@@ -181,12 +185,77 @@ int bench(const char* casePath, int steps, int warmup, int measure) {
   return 0;
 }
 
+// All cases planned up front, each tensor at its own 256-byte-aligned offset
+// of one input and one output buffer; one step = librettExecute on every
+// case in order (the per-tensor loop a grouped execution replaces).
+int loop(const char* casePath, int steps, int warmup) {
+  std::vector<Case> cases = readCases(casePath);
+  std::vector<size_t> off(cases.size());
+  size_t total = 0, algBytes = 0;
+  for (size_t n = 0; n < cases.size(); ++n) {
+    off[n] = total;
+    const size_t b = volumeOf(cases[n]) * cases[n].es;
+    algBytes += 2 * b;
+    total += (b + 255) / 256 * 256;
+  }
+  unsigned char *din, *dout;
+  CHECK(cudaMalloc(&din, total + 256));
+  CHECK(cudaMalloc(&dout, total + 256));
+  CHECK(cudaMemset(din, 0x3c, total + 256));
+  cudaStream_t s;
+  CHECK(cudaStreamCreate(&s));
+  std::vector<librettHandle> h(cases.size());
+  auto t0 = std::chrono::steady_clock::now();
+  for (size_t n = 0; n < cases.size(); ++n) {
+    Case& c = cases[n];
+    librettResult r = librettPlan(&h[n], (int)c.dim.size(), c.dim.data(), c.perm.data(), c.es, s);
+    if (r != LIBRETT_SUCCESS) {
+      std::fprintf(stderr, "case %zu: plan -> %d\n", n, (int)r);
+      return 3;
+    }
+  }
+  CHECK(cudaStreamSynchronize(s));
+  const double planS =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  auto step = [&]() {
+    for (size_t n = 0; n < cases.size(); ++n)
+      if (librettExecute(h[n], din + off[n], dout + off[n]) != LIBRETT_SUCCESS) return false;
+    return true;
+  };
+  for (int w = 0; w < warmup; ++w)
+    if (!step()) return 3;
+  CHECK(cudaStreamSynchronize(s));
+  cudaEvent_t e0, e1;
+  CHECK(cudaEventCreate(&e0));
+  CHECK(cudaEventCreate(&e1));
+  CHECK(cudaEventRecord(e0, s));
+  for (int k = 0; k < steps; ++k)
+    if (!step()) return 3;
+  CHECK(cudaEventRecord(e1, s));
+  CHECK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  CHECK(cudaEventElapsedTime(&ms, e0, e1));
+  ms /= steps;
+  std::printf("{\"mode\": \"loop\", \"transposes\": %zu, \"ms_per_step\": %.4f, "
+              "\"transposes_per_s\": %.1f, \"gbs\": %.3f, \"plan_s\": %.3f}\n",
+              cases.size(), ms, cases.size() / (ms * 1e-3), algBytes / (ms * 1e-3) / 1e9, planS);
+  std::fflush(stdout);
+  for (librettHandle x : h) librettDestroy(x);
+  CHECK(cudaFree(din));
+  CHECK(cudaFree(dout));
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc >= 5 && std::strcmp(argv[1], "loop") == 0)
+    return loop(argv[2], std::atoi(argv[3]), std::atoi(argv[4]));
   if (argc >= 4 && std::strcmp(argv[1], "golden") == 0) return golden(argv[2], argv[3]);
   if (argc >= 6 && std::strcmp(argv[1], "bench") == 0)
     return bench(argv[2], std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]));
-  std::fprintf(stderr, "usage: ref_driver golden <cases> <outdir> | bench <cases> <steps> <warmup> <measure>\n");
+  std::fprintf(stderr,
+               "usage: ref_driver golden <cases> <outdir> | bench <cases> <steps> <warmup> "
+               "<measure> | loop <cases> <steps> <warmup>\n");
   return 1;
 }

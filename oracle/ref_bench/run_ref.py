@@ -8,7 +8,9 @@ oracle/_ref/ref_driver with nvcc for sm_103a, then:
              librettPlan + librettExecute and compares the sha256 of each
              output with the fixture (pins the fixtures to LibreTT itself);
   --bench  : times LibreTT on the small case, the two small-leading-dimension
-             cases and the first --suite problems of the random-shape suite.
+             cases and the first --suite problems of the random-shape suite;
+  --loop N : times LibreTT's per-tensor librettExecute loop over N problems of
+             the batched distribution (librett_gb300.workloads).
 
 Usage: python oracle/ref_bench/run_ref.py --src <LibreTT src dir> --out <dir>
        [--golden] [--bench] [--suite N] [--measure]
@@ -87,6 +89,20 @@ def run_bench(out: Path, nsuite: int, measure: bool, steps: int = 10, warmup: in
     return lines
 
 
+def run_loop(out: Path, n: int, steps: int = 5, warmup: int = 3):
+    sys.path.insert(0, str(ROOT))
+    from librett_gb300.workloads import grouped_problems
+
+    cases = [(d, p, es, "none") for d, p, es in grouped_problems(n)]
+    cf = out / "loop_cases.txt"
+    write_cases(cf, cases)
+    res = subprocess.run([str(DRIVER), "loop", str(cf), str(steps), str(warmup)], check=True,
+                         capture_output=True, text=True)
+    line = [json.loads(x) for x in res.stdout.splitlines() if x.startswith("{")][0]
+    (out / "reference_loop.json").write_text(json.dumps(line) + "\n")
+    return line
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--src", default="/root/reference/src")
@@ -95,6 +111,9 @@ def main(argv=None):
     ap.add_argument("--bench", action="store_true")
     ap.add_argument("--measure", action="store_true", help="bench with librettPlanMeasure")
     ap.add_argument("--suite", type=int, default=40)
+    ap.add_argument("--loop", type=int, default=0,
+                    help="time LibreTT's per-tensor librettExecute loop over this many "
+                         "problems of the batched distribution")
     args = ap.parse_args(argv)
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -108,6 +127,9 @@ def main(argv=None):
         if args.measure:
             lines = run_bench(out, args.suite, True)
             print(f"bench (plan measure): {len(lines)} cases timed")
+    if args.loop:
+        line = run_loop(out, args.loop)
+        print("loop: " + json.dumps(line))
     return 0
 
 

@@ -37,11 +37,15 @@ def test_cxx_symbols_match_librett_mangling():
     exported = _exported()
     for sym in _lib.CXX_SYMBOLS:
         assert sym in exported, sym
-    # the C++ declarations of include/librett.h are exactly these six
+    # the C++ declarations of include/librett.h: LibreTT's six plus grouped execution
     text = (ROOT / "include" / "librett.h").read_text()
     decls = set(re.findall(r"^(?:void|librettResult)\s+(librett\w+)\(", text, re.M))
     assert decls == {"librettInitialize", "librettFinalize", "librettPlan", "librettPlanMeasure",
-                     "librettDestroy", "librettExecute"}
+                     "librettDestroy", "librettExecute", *_lib.CXX_GROUP_SYMBOLS}
+    demangled = subprocess.run(["nm", "-DC", "--defined-only", str(_lib.LIB_PATH)],
+                               capture_output=True, text=True, check=True).stdout
+    for name in _lib.CXX_GROUP_SYMBOLS:
+        assert re.search(rf"\b{name}\(", demangled), name
 
 
 def test_result_codes_and_strings():

@@ -1,0 +1,270 @@
+"""Grouped execution (librettGroup* / librettExecuteGrouped) against the oracle.
+
+Many uneven transposes share one input and one output buffer, each tensor at
+its own offset with a canary-filled gap behind it.  After the group runs,
+every tensor must equal the oracle's transpose bit for bit and every gap must
+still hold the canary.  Covered: mixed ranks, permutations and element sizes
+(4/8/16 bytes); members whose pointers are not 16-byte aligned (element
+units inside their bucket); a member needing more grid ranks than the
+compact descriptor holds (its plan's own launch inside the graph); a second
+execution after the inputs changed (the graph reads the buffers anew); plans
+destroyed before the group runs; every tile policy and the autotuner; the
+one-shot librettExecuteGrouped; the plain per-tensor loop; and the error
+codes.
+"""
+import numpy as np
+import pytest
+
+import librett_gb300 as L
+from librett_gb300.workloads import grouped_problems
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+CANARY = 0x5A
+GAP = 64
+
+
+def _layout(problems, misalign):
+    """Byte offsets: 256-aligned starts plus, for members flagged in
+    `misalign`, a shift by one element (4 or 8 bytes)."""
+    offs, total = [], 0
+    for (dims, _, es), mis in zip(problems, misalign):
+        start = total + (es if mis else 0)
+        offs.append(start)
+        nb = int(np.prod(dims)) * es
+        total = (start + nb + GAP + 255) // 256 * 256
+    return offs, total
+
+
+def _mixed_problems(n, seed):
+    probs = grouped_problems(n, seed=seed, log2_lo=4, log2_hi=15, sizes=(4, 8, 16), max_rank=6)
+    probs.append(([2, 3] * 8, [int(x) for x in np.random.default_rng(seed).permutation(16)], 4))
+    probs.append(([5], [0], 8))                      # rank 1: a plain copy
+    probs.append(([7, 1, 9, 1], [3, 2, 1, 0], 16))   # unit dims fuse away
+    return probs
+
+
+class _Batch:
+    def __init__(self, probs, misalign, seed):
+        import torch
+
+        self.probs = probs
+        self.offs, total = _layout(probs, misalign)
+        self.total = total
+        self.rng = np.random.default_rng(seed)
+        self.inp = torch.zeros(total, dtype=torch.uint8, device="cuda")
+        self.out = torch.full((total,), CANARY, dtype=torch.uint8, device="cuda")
+        self.host = None
+        self.refill()
+
+    def refill(self):
+        import torch
+
+        self.host = self.rng.integers(0, 256, self.total, dtype=np.uint8)
+        self.inp.copy_(torch.from_numpy(self.host))
+
+    def ptrs(self):
+        return ([self.inp.data_ptr() + o for o in self.offs],
+                [self.out.data_ptr() + o for o in self.offs])
+
+    def check(self):
+        import torch
+
+        torch.cuda.synchronize()
+        res = self.out.cpu().numpy()
+        covered = np.zeros(self.total, dtype=bool)
+        for i, ((dims, perm, es), o) in enumerate(zip(self.probs, self.offs)):
+            nb = int(np.prod(dims)) * es
+            want = O.transpose_np(self.host[o:o + nb], dims, perm, es).view(np.uint8)
+            got = res[o:o + nb]
+            if not np.array_equal(got, want):
+                bad = int(np.nonzero(got != want)[0][0])
+                raise AssertionError(f"member {i} dims {dims} perm {perm} es {es}: byte {bad}")
+            covered[o:o + nb] = True
+        assert (res[~covered] == CANARY).all(), "write outside the members' outputs"
+
+
+def _plans(probs, stream):
+    return [L.Plan(d, p, es, stream) for d, p, es in probs]
+
+
+def test_group_mixed_bit_exact(cuda):
+    import torch
+
+    probs = _mixed_problems(400, seed=11)
+    rng = np.random.default_rng(5)
+    misalign = [bool(rng.random() < 0.15) and es < 16 for _, _, es in probs]
+    b = _Batch(probs, misalign, seed=3)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    before = L.launch_count()
+    with L.Group(plans, ins, outs, stream) as g:
+        info = g.info()
+        assert info["members"] == len(probs)
+        assert info["bytes"] == sum(2 * int(np.prod(d)) * es for d, _, es in probs)
+        launches = L.launch_count()
+        g.execute()
+        assert L.launch_count() - launches == info["buckets"] + info["separate"]
+        b.check()
+        b.refill()
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
+    assert L.launch_count() > before
+
+
+def test_group_separate_member(cuda):
+    import torch
+
+    # 16 unfusable ranks: every flat tile leaves more than eight grid ranks
+    probs = [([3] * 16, list(range(15, -1, -1)), 4)] + _mixed_problems(20, seed=21)
+    b = _Batch(probs, [False] * len(probs), seed=9)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream) as g:
+        assert g.info()["separate"] == 1
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
+
+
+@pytest.mark.parametrize("policy", [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2), (3, 3, 3, 3),
+                                    (2, 0, 3, 1)])
+def test_group_policies(cuda, policy):
+    import torch
+
+    probs = _mixed_problems(150, seed=16)
+    rng = np.random.default_rng(17)
+    misalign = [bool(rng.random() < 0.2) and es < 16 for _, _, es in probs]
+    b = _Batch(probs, misalign, seed=10)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream, policy=policy) as g:
+        assert g.policy() == (list(policy), False)
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_group_tune_and_cache(cuda):
+    import torch
+
+    probs = grouped_problems(300, seed=18, log2_lo=10, log2_hi=18)
+    b = _Batch(probs, [False] * len(probs), seed=11)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream) as g:
+        g.tune()
+        pol, tuned = g.policy()
+        assert tuned and all(0 <= x < 4 for x in pol)
+        b.out.fill_(CANARY)
+        g.execute()
+        b.check()
+    # a new group over the same batch starts from the tuned policy
+    with L.Group(plans, ins, outs, stream) as g2:
+        assert g2.policy() == (pol, True)
+    for p in plans:
+        p.destroy()
+
+
+def test_group_outlives_its_plans(cuda):
+    import torch
+
+    probs = _mixed_problems(120, seed=12)
+    b = _Batch(probs, [False] * len(probs), seed=4)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    g = L.Group(plans, ins, outs, stream)
+    for p in plans:
+        p.destroy()
+    g.execute()
+    b.check()
+    g.destroy()
+
+
+def test_group_on_side_stream(cuda):
+    import torch
+
+    probs = _mixed_problems(60, seed=13)
+    b = _Batch(probs, [False] * len(probs), seed=6)
+    side = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    plans = _plans(probs, side)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, side) as g:
+        g.execute()
+        side.synchronize()
+        b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_execute_grouped_one_shot(cuda):
+    import torch
+
+    probs = _mixed_problems(80, seed=14)
+    b = _Batch(probs, [False] * len(probs), seed=7)
+    plans = _plans(probs, torch.cuda.current_stream())
+    ins, outs = b.ptrs()
+    L.execute_grouped(plans, ins, outs)
+    b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_execute_batch_loop(cuda):
+    import torch
+
+    probs = _mixed_problems(80, seed=15)
+    b = _Batch(probs, [False] * len(probs), seed=8)
+    plans = _plans(probs, torch.cuda.current_stream())
+    ins, outs = b.ptrs()
+    L.execute_batch(plans, ins, outs)
+    b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_group_errors(cuda):
+    import ctypes
+
+    import torch
+
+    lib = L._lib.load()
+    s = torch.cuda.current_stream()
+    buf = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+    out = torch.zeros(4096, dtype=torch.uint8, device="cuda")
+    with L.Plan([8, 16], [1, 0], 4, s) as p:
+        with pytest.raises(L.LibrettError) as e:
+            L.Group([p], [buf.data_ptr()], [buf.data_ptr()], s)
+        assert e.value.code == L.LIBRETT_INVALID_PARAMETER
+        with pytest.raises(L.LibrettError) as e:
+            L.Group([p], [buf.data_ptr() + 2], [out.data_ptr()], s)  # not 4-byte aligned
+        assert e.value.code == L.LIBRETT_INVALID_PARAMETER
+        with pytest.raises(L.LibrettError) as e:
+            L.Group([123456789], [buf.data_ptr()], [out.data_ptr()], s)
+        assert e.value.code == L.LIBRETT_INVALID_PLAN
+        with pytest.raises(L.LibrettError) as e:
+            L.execute_batch([p, p], [buf.data_ptr(), buf.data_ptr()],
+                            [out.data_ptr(), buf.data_ptr()])
+        assert e.value.code == L.LIBRETT_INVALID_PARAMETER
+    h = ctypes.c_uint(0)
+    assert lib.librett_c_group_create(ctypes.byref(h), 0, None, None, None,
+                                      ctypes.c_void_p(s.cuda_stream)) == L.LIBRETT_INVALID_PARAMETER
+    assert lib.librett_c_group_execute(987654) == L.LIBRETT_INVALID_PLAN
+    assert lib.librett_c_group_destroy(987654) == L.LIBRETT_INVALID_PLAN
+    assert lib.librett_c_execute_grouped(0, None, None, None) == L.LIBRETT_INVALID_PARAMETER
+    assert lib.librett_c_group_tune(987654) == L.LIBRETT_INVALID_PLAN
+    with L.Plan([8, 16], [1, 0], 4, s) as p:
+        with pytest.raises(L.LibrettError) as e:
+            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 7, 0))
+        assert e.value.code == L.LIBRETT_INVALID_PARAMETER
