@@ -503,7 +503,7 @@ def run_grouped(args):
     plans = [L.Plan(d, p, es, stream) for d, p, es in problems]
     plan_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    grp = L.Group(plans, ins, outs, stream)
+    grp = L.Group(plans, ins, outs, stream, policy=args.policy)
     create_s = time.perf_counter() - t0
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
@@ -521,12 +521,16 @@ def run_grouped(args):
     grp.execute()
     untuned_ms = time_group(max(1, args.steps))
     tune_s = None
-    if not args.no_tune:
+    if not args.no_tune and args.policy is None:
         t0 = time.perf_counter()
         grp.tune()
         tune_s = time.perf_counter() - t0
     policy, tuned = grp.policy()
     ginfo = grp.info()
+    if args.buckets:
+        with open(args.buckets, "w") as fb:
+            for b in grp.buckets():
+                fb.write(json.dumps(b) + "\n")
     step_bytes = ginfo["bytes"]
 
     for _ in range(args.warmup):
@@ -666,6 +670,10 @@ def main(argv=None):
                     help="seconds of host gather for the cpu_baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--buckets", type=str, default=None,
+                    help="grouped workload: write the graph's bucket launches (JSON lines)")
+    ap.add_argument("--policy", type=str, default=None,
+                    help="grouped workload: tile policy per size class, e.g. 0,1,1,0 (no tuning)")
     ap.add_argument("--no-tune", action="store_true",
                     help="grouped workload: keep the plan selector's tiles (no autotuning)")
     ap.add_argument("--dims", type=str, default=None, help="custom problem: comma-separated dims")
@@ -681,6 +689,8 @@ def main(argv=None):
         args.workload = "custom"
         args.custom = ([int(x) for x in args.dims.split(",")],
                        [int(x) for x in args.perm.split(",")], args.es)
+    if args.policy is not None:
+        args.policy = [int(x) for x in args.policy.split(",")]
     if args.problems is None:
         args.problems = 10000 if args.workload == "grouped" else 200
     if args.impl == "reference":

@@ -164,14 +164,22 @@ typedef unsigned int librettGroupHandle;
 #endif
 int librett_c_group_create(librettGroupHandle* group, int count, const librettHandle* plans,
                            void* const* idata, void* const* odata, void* stream);
-/* As librett_c_group_create with the tile policy given per member size
- * class (policy[4]: classes < 64 KiB, < 1 MiB, < 16 MiB, larger; values
- * 0 = plan selector's tile, 1 = largest tile within 10% of the best sector
- * efficiency, 2 = largest tile, 3 = analytic model for a full device). */
+/* As librett_c_group_create with the policy given per member size class
+ * (policy[4]: classes < 64 KiB, < 1 MiB, < 16 MiB, larger).  A policy is
+ * tile + 4 * loads: tile 0 = plan selector's tile, 1 = largest tile within
+ * 10% of the best sector efficiency, 2 = largest tile, 3 = analytic model for
+ * a full device; loads 0 = through registers, 1 = cp.async into shared
+ * memory.  Values 0..7. */
 int librett_c_group_create_policy(librettGroupHandle* group, int count,
                                   const librettHandle* plans, void* const* idata,
                                   void* const* odata, void* stream, const int* policy);
 int librett_c_group_tune(librettGroupHandle group);
+/* Bucket `index` (launch order) of the group's graph: shape[6] = element
+ * bytes, load unit, store unit (elements), load units per thread, dynamic
+ * shared memory bytes, cp.async loads (0/1); its members, tiles and
+ * algorithmic bytes. */
+int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int* members,
+                           long long* tiles, long long* bytes);
 /* policy[4] in use, and whether it came from tuning (this group's or a
  * cached one for the same batch signature). */
 int librett_c_group_policy(librettGroupHandle group, int* policy, int* tuned);
@@ -179,6 +187,17 @@ int librett_c_group_execute(librettGroupHandle group);
 int librett_c_group_destroy(librettGroupHandle group);
 int librett_c_execute_grouped(int count, const librettHandle* plans, void* const* idata,
                               void* const* odata);
+/* Host-only self-check of grouped execution's run tables for flat-tile
+ * candidate `candidate` (in element units when element_units != 0): the
+ * kernel's run-split index arithmetic must reproduce the per-unit offset
+ * tables of the single-plan kernel for every unit of the tile.  Returns
+ * LIBRETT_SUCCESS when it does, LIBRETT_INTERNAL_ERROR on a mismatch,
+ * LIBRETT_INVALID_DEVICE when the tile's vector units cross a run (the group
+ * then moves that member in element units), LIBRETT_INVALID_PARAMETER for a
+ * bad problem or candidate. */
+int librett_c_group_run_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                              int num_sms, int candidate, int element_units);
+
 /* The plain per-tensor loop the grouped path replaces: librettExecute on
  * each (plan, idata, odata) in order, one launch each; stops at and returns
  * the first error. */

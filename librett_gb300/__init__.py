@@ -127,8 +127,9 @@ class Group:
     """Owning wrapper of a group of plans executed as one CUDA graph
     (librett_c_group_*; no LibreTT counterpart)."""
 
-    # tile policies per member size class (librett_c.h)
+    # policies per member size class (librett_c.h): tile + 4 * loads
     POLICY_SELECTOR, POLICY_WIDE, POLICY_WIDEST, POLICY_FILL = 0, 1, 2, 3
+    LOADS_REGISTERS, LOADS_ASYNC = 0, 4
 
     def __init__(self, plans, idata, odata, stream=None, *, policy=None):
         n, hs, ins, outs = _handle_arrays(plans, idata, odata)
@@ -149,6 +150,22 @@ class Group:
         rc = _lib.load().librett_c_group_tune(self.handle)
         if rc != LIBRETT_SUCCESS:
             raise LibrettError(rc, "librett_c_group_tune")
+
+    def buckets(self) -> list[dict]:
+        """The graph's bucket launches in launch order."""
+        out = []
+        lib = _lib.load()
+        for b in range(self.info()["buckets"]):
+            shape = (ctypes.c_int * 6)()
+            m, t, by = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+            rc = lib.librett_c_group_bucket(self.handle, b, shape, ctypes.byref(m), ctypes.byref(t),
+                                            ctypes.byref(by))
+            if rc != LIBRETT_SUCCESS:
+                raise LibrettError(rc, "librett_c_group_bucket")
+            out.append({"es": shape[0], "lv": shape[1], "sv": shape[2], "nl": shape[3],
+                        "smem": shape[4], "async": shape[5], "members": m.value, "tiles": t.value,
+                        "bytes": by.value})
+        return out
 
     def policy(self) -> tuple[list[int], bool]:
         pol = (ctypes.c_int * 4)()

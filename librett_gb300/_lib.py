@@ -117,12 +117,18 @@ C_FUNCTIONS = [
      [ctypes.POINTER(_H), ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P),
       ctypes.POINTER(_P), _P, ctypes.POINTER(ctypes.c_int)]),
     ("librett_c_group_tune", ctypes.c_int, [_H]),
+    ("librett_c_group_bucket", ctypes.c_int,
+     [_H, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+      ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_group_policy", ctypes.c_int,
      [_H, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     ("librett_c_group_execute", ctypes.c_int, [_H]),
     ("librett_c_group_destroy", ctypes.c_int, [_H]),
     ("librett_c_execute_grouped", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    ("librett_c_group_run_check", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
+      ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     ("librett_c_execute_batch", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     ("librett_c_group_info", ctypes.c_int,

@@ -161,7 +161,6 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   bool learned = false;
   int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName.c_str(), &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
-  if (!lt::finalizePlan(cands[pick])) return LIBRETT_INTERNAL_ERROR;
   return activate(handle, cands[pick], stream, dev, sms, candidate >= 0 ? 3 : (learned ? 1 : 0));
 }
 
@@ -262,6 +261,7 @@ librettResult librettExecute(librettHandle handle, void* idata, void* odata) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   if (dev != obj->device) return LIBRETT_INVALID_DEVICE;
+  if (obj->needsScalar(idata, odata) && !obj->ensureScalar()) return LIBRETT_INTERNAL_ERROR;
   int grid = 0;
   if (lt::launchPlan(obj->pd, &obj->tables, idata, odata, obj->stream, obj->numSMs, &grid) !=
       cudaSuccess)
@@ -329,6 +329,51 @@ int librett_c_describe(int rank, const int* dim, const int* permutation, size_t 
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
   fillInfo(cands[pick], 0, info);
   info->selected_by = candidate >= 0 ? 3 : (learned ? 1 : 0);
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_group_run_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                              int num_sms, int candidate, int element_units) {
+  if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
+  std::vector<lt::PlanDesc> cands = lt::flatTileCandidates(f, num_sms > 0 ? num_sms : 152);
+  if (candidate < 0 || candidate >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  lt::PlanDesc pd = cands[candidate];
+  if (element_units) {
+    if (!lt::finalizePlan(pd)) return LIBRETT_INTERNAL_ERROR;
+    pd.tile = pd.tileScalar;
+  }
+  const lt::TileParams& tp = pd.tile;
+  const lt::GroupRunSplit rs = lt::groupRunSplit(tp);
+  if (rs.inRun < 1 || rs.outRun < 1 || tp.tileVol % rs.inRun || tp.tileVol % rs.outRun)
+    return LIBRETT_UNDEFINED_ERROR;
+  if (rs.inRun % tp.lv || rs.outRun % tp.sv) return LIBRETT_INVALID_DEVICE;  // not applicable
+  std::vector<int> ldOff(tp.nIn), stOff(tp.nOut);
+  std::vector<unsigned short> stSm(tp.tileVol);
+  lt::tileTablesHost(tp, ldOff.data(), stOff.data(), stSm.data());
+  std::vector<int> ldRow(tp.tileVol / rs.inRun), stRow(tp.tileVol / rs.outRun),
+      smRow(tp.tileVol / rs.outRun), smRun(rs.outRun);
+  lt::groupRunTablesHost(tp, rs, ldRow.data(), stRow.data(), smRow.data(), smRun.data());
+  const lt::FastDiv inRun = lt::makeFastDiv((uint32_t)rs.inRun);
+  const lt::FastDiv outRun = lt::makeFastDiv((uint32_t)rs.outRun);
+  auto pad = [&](int j) { return j + ((j >> tp.padShift) << tp.padLog); };
+  // the kernel's index arithmetic, unit by unit
+  for (int u = 0; u < tp.nIn; ++u) {
+    const int j = u * tp.lv;
+    const uint32_t r = lt::fastDivHost((uint32_t)j, inRun);
+    const int a = j - (int)(r * inRun.d);
+    if (r >= ldRow.size() || a + ldRow[r] != ldOff[u]) return LIBRETT_INTERNAL_ERROR;
+  }
+  for (int w = 0; w < tp.nOut; ++w) {
+    const int q = w * tp.sv;
+    const uint32_t r = lt::fastDivHost((uint32_t)q, outRun);
+    const int a = q - (int)(r * outRun.d);
+    if (r >= stRow.size() || a + tp.sv > rs.outRun || a + stRow[r] != stOff[w])
+      return LIBRETT_INTERNAL_ERROR;
+    for (int i = 0; i < tp.sv; ++i)
+      if (pad(smRow[r] + smRun[a + i]) != stSm[q + i]) return LIBRETT_INTERNAL_ERROR;
+  }
   return LIBRETT_SUCCESS;
 }
 

@@ -27,45 +27,73 @@ namespace lt {
 extern std::atomic<unsigned long long> gLaunchCount;
 namespace {
 
-// Writes every member's offset tables (same arithmetic as
-// writeTileTablesKernel); CTA b handles member b.
+// Writes every member's run tables; CTA b handles member b.
 __global__ void __launch_bounds__(256) writeGroupTablesKernel(const GroupTableJob* __restrict__ jobs) {
   const GroupTableJob& jb = jobs[blockIdx.x];
   const TileParams& p = jb.tp;
-  for (int u = threadIdx.x; u < p.nIn; u += blockDim.x) {
-    int rem = u * p.lv, off = 0;
-    for (int t = 0; t < p.nTR; ++t) {
+  const GroupRunSplit rs = jb.rs;
+  const int nL = p.tileVol / rs.inRun, nS = p.tileVol / rs.outRun;
+  for (int r = threadIdx.x; r < nL; r += blockDim.x) {
+    int rem = r, off = 0;
+    for (int t = rs.kIn; t < p.nTR; ++t) {
       const int e = p.trE[t];
       const int q = rem / e;
       off += (rem - q * e) * p.trSin[t];
       rem = q;
     }
-    jb.ldOff[u] = off;
+    jb.ldRow[r] = off;
   }
-  for (int q = threadIdx.x; q < p.tileVol; q += blockDim.x) {
-    int rem = q, off = 0, jj = 0;
-    for (int i = 0; i < p.nTR; ++i) {
+  for (int r = threadIdx.x; r < nS; r += blockDim.x) {
+    int rem = r, off = 0, jj = 0;
+    for (int i = rs.kOut; i < p.nTR; ++i) {
       const int t = p.trOut[i];
       const int e = p.trE[t];
-      const int d = rem / e;
-      const int c = rem - d * e;
-      rem = d;
+      const int q = rem / e;
+      const int c = rem - q * e;
+      rem = q;
       off += c * p.trSout[t];
       jj += c * p.trInTile[t];
     }
-    jb.stSm[q] = (unsigned short)(jj + ((jj >> p.padShift) << p.padLog));
-    if (q % p.sv == 0) jb.stOff[q / p.sv] = off;
+    jb.stRow[r] = off;
+    jb.smRow[r] = jj;
+  }
+  for (int a = threadIdx.x; a < rs.outRun; a += blockDim.x) {
+    int rem = a, jj = 0;
+    for (int i = 0; i < rs.kOut; ++i) {
+      const int t = p.trOut[i];
+      const int e = p.trE[t];
+      const int q = rem / e;
+      jj += (rem - q * e) * p.trInTile[t];
+      rem = q;
+    }
+    jb.smRun[a] = jj;
   }
 }
 
-// Tile policies: how a member's flat tile is chosen from its candidates.
+size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+// Bytes of a member's run tables; sub-table offsets (16-byte aligned).
+size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[4]) {
+  const size_t nL = tp.tileVol / rs.inRun, nS = tp.tileVol / rs.outRun;
+  off[0] = 0;
+  off[1] = align16(4 * nL);
+  off[2] = off[1] + align16(4 * nS);
+  off[3] = off[2] + align16(4 * nS);
+  return off[3] + align16(4 * (size_t)rs.outRun);
+}
+
+// Policies: policy % GP_TILES picks a member's flat tile from its
+// candidates; policy / GP_TILES picks the bucket's loads (0 registers,
+// 1 cp.async).
 enum GroupPolicy {
   GP_SELECTOR = 0,  // the plan selector's choice for the tensor on its own
   GP_WIDE = 1,      // the largest tile within 10% of the best sector efficiency
   GP_WIDEST = 2,    // the largest tile
   GP_FILL = 3,      // the analytic model with the device assumed full of other work
-  GP_COUNT = 4
+  GP_TILES = 4,
+  GP_COUNT = 2 * GP_TILES
 };
+constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
 
 // Member size classes (bytes of one tensor): < 64 KiB, < 1 MiB, < 16 MiB, larger.
 int sizeClass(long long bytes) {
@@ -85,12 +113,18 @@ struct Member {
   PlanDesc pd;       // flat tile plan inside a bucket
 };
 
+struct BucketSummary {
+  int es, lv, sv, nl, async, members, smem;
+  long long tiles, bytes;
+};
+
 struct Build {
   void* alloc = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int buckets = 0, separate = 0;
   long long tiles = 0;
+  std::vector<BucketSummary> summary;  // in launch order
 };
 
 void releaseBuild(Build& b, cudaStream_t s) {
@@ -139,8 +173,6 @@ std::atomic<librettGroupHandle> gNextGroup{0};
 std::mutex gTuneMu;
 std::unordered_map<uint64_t, Policy> gTuneCache;
 
-size_t align16(size_t x) { return (x + 15) / 16 * 16; }
-
 uint64_t fnv(uint64_t h, uint64_t v) {
   for (int i = 0; i < 8; ++i) {
     h ^= (v >> (8 * i)) & 0xff;
@@ -149,12 +181,12 @@ uint64_t fnv(uint64_t h, uint64_t v) {
   return h;
 }
 
-cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, const GroupTensor* tens,
+cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, bool async, const GroupTensor* tens,
                               const int* map, uint32_t tiles, int smem, cudaStream_t s) {
   switch (es) {
-    case 4: return launchGroupTile4(lv, sv, nl, tens, map, tiles, smem, s);
-    case 8: return launchGroupTile8(lv, sv, nl, tens, map, tiles, smem, s);
-    case 16: return launchGroupTile16(lv, sv, nl, tens, map, tiles, smem, s);
+    case 4: return launchGroupTile4(lv, sv, nl, async, tens, map, tiles, smem, s);
+    case 8: return launchGroupTile8(lv, sv, nl, async, tens, map, tiles, smem, s);
+    case 16: return launchGroupTile16(lv, sv, nl, async, tens, map, tiles, smem, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -162,6 +194,7 @@ cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, const GroupTensor*
 // Flat tile plan of member m under a policy; false when the member must run
 // its plan's own launch.
 bool pickTile(const Member& m, int policy, int sms, const std::string& dev, PlanDesc& out) {
+  policy %= GP_TILES;
   const PlanDesc& own = m.plan->pd;
   if (policy == GP_SELECTOR && own.kernel == K_TILE && own.pipe == PIPE_FLAT) {
     out = own;
@@ -198,8 +231,11 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     }
     out = c[k];
   }
-  if (!m.aligned16 && (out.tile.lv > 1 || out.tile.sv > 1)) {
-    // pointers not 16-byte aligned: the same tile in element units
+  const GroupRunSplit rs = groupRunSplit(out.tile);
+  const bool unitsFit = rs.inRun % out.tile.lv == 0 && rs.outRun % out.tile.sv == 0;
+  if ((!m.aligned16 || !unitsFit) && (out.tile.lv > 1 || out.tile.sv > 1)) {
+    // pointers not 16-byte aligned, or vector units that would cross a run:
+    // the same tile in element units
     if (!finalizePlan(out)) return false;
     out.tile = out.tileScalar;
     out.slots = out.slotsScalar;
@@ -209,7 +245,7 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
 }
 
 struct Bucket {
-  int es, lv, sv, nl;
+  int es, lv, sv, nl, async;
   int smem = 0;
   uint32_t tiles = 0;
   long long bytes = 0;
@@ -221,7 +257,7 @@ struct Bucket {
 // group's stream.
 librettResult build(GroupObj& g, const Policy& pol) {
   for (Member& m : g.members) {
-    const int p = pol[m.cls];
+    const int p = pol[m.cls] % GP_TILES;
     if (m.picked == p) continue;
     m.separate = !pickTile(m, p, g.numSMs, g.devName, m.pd);
     m.picked = p;
@@ -232,16 +268,20 @@ librettResult build(GroupObj& g, const Policy& pol) {
   Build& B = g.built;
 
   // buckets by kernel shape
-  std::map<std::tuple<int, int, int, int>, int> key2b;
+  std::map<std::tuple<int, int, int, int, int, int>, int> key2b;
   std::vector<Bucket> buckets;
   for (int i = 0; i < (int)g.members.size(); ++i) {
     const Member& m = g.members[i];
     if (m.separate) {
+      if (m.plan->needsScalar(m.in, m.out) && !m.plan->ensureScalar())
+        return LIBRETT_INTERNAL_ERROR;
       ++B.separate;
       continue;
     }
     const PlanDesc& pd = m.pd;
-    auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots);
+    const int async = pol[m.cls] / GP_TILES;
+    auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots, async,
+                               (pd.smemBytes + SMEM_CLASS - 1) / SMEM_CLASS);
     auto it = key2b.find(key);
     if (it == key2b.end()) {
       Bucket b;
@@ -249,6 +289,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       b.lv = pd.tile.lv;
       b.sv = pd.tile.sv;
       b.nl = pd.slots;
+      b.async = async;
       it = key2b.emplace(key, (int)buckets.size()).first;
       buckets.push_back(b);
     }
@@ -283,9 +324,10 @@ librettResult build(GroupObj& g, const Policy& pol) {
   std::vector<size_t> tabOff(g.members.size(), 0);
   for (const Bucket& b : buckets)
     for (int i : b.members) {
-      size_t so, smo;
+      size_t sub[4];
+      const TileParams& tp = g.members[i].pd.tile;
       tabOff[i] = off;
-      off = align16(off + deviceTableBytes(g.members[i].pd.tile, &so, &smo));
+      off = align16(off + runTableBytes(tp, groupRunSplit(tp), sub));
     }
   const size_t total = std::max<size_t>(off, 16);
   if (cudaMallocAsync(&B.alloc, total, g.stream) != cudaSuccess) {
@@ -303,19 +345,23 @@ librettResult build(GroupObj& g, const Policy& pol) {
       const int i = b.members[k];
       const Member& m = g.members[i];
       const TileParams& tp = m.pd.tile;
-      size_t so, smo;
-      deviceTableBytes(tp, &so, &smo);
+      const GroupRunSplit rs = groupRunSplit(tp);
+      size_t sub[4];
+      runTableBytes(tp, rs, sub);
       unsigned char* tb = base + tabOff[i];
       GroupTensor& t = tens[k];
       std::memset(&t, 0, sizeof(t));
       t.in = m.in;
       t.out = m.out;
-      t.ldOff = reinterpret_cast<const int*>(tb);
-      t.stOff = reinterpret_cast<const int*>(tb + so);
-      t.stSm = reinterpret_cast<const unsigned short*>(tb + smo);
+      t.ldRow = reinterpret_cast<const int*>(tb + sub[0]);
+      t.stRow = reinterpret_cast<const int*>(tb + sub[1]);
+      t.smRow = reinterpret_cast<const int*>(tb + sub[2]);
+      t.smRun = reinterpret_cast<const int*>(tb + sub[3]);
       t.firstTile = first;
       t.nIn = tp.nIn;
       t.nOut = tp.nOut;
+      t.inRun = makeFastDiv((uint32_t)rs.inRun);
+      t.outRun = makeFastDiv((uint32_t)rs.outRun);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
       t.nGR = tp.nGR;
@@ -331,9 +377,11 @@ librettResult build(GroupObj& g, const Policy& pol) {
       GroupTableJob jb;
       std::memset(&jb, 0, sizeof(jb));
       jb.tp = tp;
-      jb.ldOff = reinterpret_cast<int*>(tb);
-      jb.stOff = reinterpret_cast<int*>(tb + so);
-      jb.stSm = reinterpret_cast<unsigned short*>(tb + smo);
+      jb.rs = rs;
+      jb.ldRow = reinterpret_cast<int*>(tb + sub[0]);
+      jb.stRow = reinterpret_cast<int*>(tb + sub[1]);
+      jb.smRow = reinterpret_cast<int*>(tb + sub[2]);
+      jb.smRun = reinterpret_cast<int*>(tb + sub[3]);
       std::memcpy(jobs + jobOf[i], &jb, sizeof(jb));
     }
   }
@@ -384,7 +432,9 @@ librettResult build(GroupObj& g, const Policy& pol) {
       load[br] += nd.bytes;
       if (nd.bucket >= 0) {
         const Bucket& b = buckets[nd.bucket];
-        launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl,
+        B.summary.push_back({b.es, b.lv, b.sv, b.nl, b.async, (int)b.members.size(), b.smem,
+                             (long long)b.tiles, b.bytes});
+        launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl, b.async != 0,
                                      reinterpret_cast<const GroupTensor*>(base + b.tensOff),
                                      reinterpret_cast<const int*>(base + b.mapOff), b.tiles,
                                      b.smem, side[br]) == cudaSuccess;
@@ -462,8 +512,11 @@ librettResult create(librettGroupHandle* handle, int count, const librettHandle*
     m.aligned16 = (uintptr_t)m.in % 16 == 0 && (uintptr_t)m.out % 16 == 0;
   }
   g->signature = batchSignature(*g);
+  // Untuned default: the largest tiles, loaded by cp.async (the fastest
+  // uniform policy on the 10,000-tensor batch of rank 2..6, 2^10..2^22
+  // elements, f32/f64).
   Policy pol;
-  pol.fill(GP_SELECTOR);
+  pol.fill(GP_WIDEST + GP_TILES);
   if (policy != nullptr) {
     std::copy(policy, policy + GROUP_CLASSES, pol.begin());
   } else {
@@ -524,10 +577,13 @@ bool timeBuild(GroupObj& g, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
   return true;
 }
 
-// Coordinate descent over the size classes (largest first): each class
-// tries every policy with the others fixed and keeps one that is at least 2%
-// faster.  Times on the group's own buffers (reads the inputs, overwrites
-// the outputs); the result is cached by batch signature.
+// Autotuner.  Phase 1 times every policy applied to all size classes and
+// keeps the fastest; phase 2 walks the classes that hold at least 2% of the
+// group's bytes (largest class first) and tries, for one class at a time,
+// the other tile choices with the same loads and the other loads with the
+// same tile, keeping a change that is at least 2% faster.  Times on the
+// group's own buffers (reads the inputs, overwrites the outputs); the result
+// is cached by batch signature.
 librettResult tune(librettGroupHandle h) {
   std::shared_ptr<GroupObj> gp = findGroup(h);
   if (!gp) return LIBRETT_INVALID_PLAN;
@@ -535,8 +591,9 @@ librettResult tune(librettGroupHandle h) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   if (dev != g.device) return LIBRETT_INVALID_DEVICE;
-  bool present[GROUP_CLASSES] = {};
-  for (const Member& m : g.members) present[m.cls] = true;
+  long long classBytes[GROUP_CLASSES] = {};
+  for (const Member& m : g.members)
+    classBytes[m.cls] += 2 * m.plan->pd.f.vol * (long long)m.plan->pd.f.esize;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
     if (e0) cudaEventDestroy(e0);
@@ -544,20 +601,37 @@ librettResult tune(librettGroupHandle h) {
   }
   librettResult r = LIBRETT_SUCCESS;
   Policy cur = g.policy;
-  float best = 0.f;
-  if (!timeBuild(g, e0, e1, &best)) r = LIBRETT_INTERNAL_ERROR;
+  float best = -1.f;
+  auto trial = [&](const Policy& pol) {
+    float t = 0.f;
+    r = build(g, pol);
+    if (r == LIBRETT_SUCCESS && !timeBuild(g, e0, e1, &t)) r = LIBRETT_INTERNAL_ERROR;
+    return r == LIBRETT_SUCCESS ? t : -1.f;
+  };
+  for (int p = 0; p < GP_COUNT && r == LIBRETT_SUCCESS; ++p) {
+    Policy pol;
+    pol.fill(p);
+    const float t = trial(pol);
+    if (r == LIBRETT_SUCCESS && (best < 0.f || t < best)) {
+      best = t;
+      cur = pol;
+    }
+  }
   for (int c = GROUP_CLASSES - 1; c >= 0 && r == LIBRETT_SUCCESS; --c) {
-    if (!present[c]) continue;
-    for (int p = 0; p < GP_COUNT && r == LIBRETT_SUCCESS; ++p) {
-      if (p == cur[c]) continue;
-      Policy trial = cur;
-      trial[c] = p;
-      float t = 0.f;
-      r = build(g, trial);
-      if (r == LIBRETT_SUCCESS && !timeBuild(g, e0, e1, &t)) r = LIBRETT_INTERNAL_ERROR;
-      if (r == LIBRETT_SUCCESS && t < 0.98f * best) {
+    if (classBytes[c] * 50 < g.bytes) continue;
+    const int tile = cur[c] % GP_TILES, loads = cur[c] / GP_TILES;
+    std::vector<int> alts;
+    for (int t = 0; t < GP_TILES; ++t)
+      if (t != tile) alts.push_back(t + GP_TILES * loads);
+    alts.push_back(tile + GP_TILES * (1 - loads));
+    for (int p : alts) {
+      Policy pol = cur;
+      pol[c] = p;
+      const float t = trial(pol);
+      if (r != LIBRETT_SUCCESS) break;
+      if (t < 0.98f * best) {
         best = t;
-        cur = trial;
+        cur = pol;
       }
     }
   }
@@ -653,6 +727,26 @@ int librett_c_group_info(librettGroupHandle group, int* members, int* buckets, i
   if (separate) *separate = g->built.separate;
   if (tiles) *tiles = g->built.tiles;
   if (bytes) *bytes = g->bytes;
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int* members,
+                           long long* tiles, long long* bytes) {
+  std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
+  if (!g) return LIBRETT_INVALID_PLAN;
+  if (index < 0 || index >= (int)g->built.summary.size()) return LIBRETT_INVALID_PARAMETER;
+  const lt::BucketSummary& b = g->built.summary[index];
+  if (shape) {
+    shape[0] = b.es;
+    shape[1] = b.lv;
+    shape[2] = b.sv;
+    shape[3] = b.nl;
+    shape[4] = b.smem;
+    shape[5] = b.async;
+  }
+  if (members) *members = b.members;
+  if (tiles) *tiles = b.tiles;
+  if (bytes) *bytes = b.bytes;
   return LIBRETT_SUCCESS;
 }
 

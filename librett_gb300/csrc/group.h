@@ -9,9 +9,12 @@
 // (pointers, offset tables, grid-rank decode).  Members that do not fit the
 // compact descriptor run with their own launch inside the same graph.
 //
-// Which flat tile a member gets is a policy per member size class; an
-// autotuner (librettGroupTune) times the policies on the group's own buffers
-// and keeps the fastest combination, cached by the batch's signature.
+// Which flat tile a member gets, and whether its bucket loads through
+// registers or cp.async, is a policy per member size class; an autotuner
+// (librettGroupTune) times the policies on the group's own buffers and keeps
+// the fastest combination, cached by the batch's signature.  Buckets are
+// also split by shared-memory size (4 KiB classes), so that a CTA reserves
+// little more than its own tile needs.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -28,11 +31,13 @@ constexpr int GROUP_CLASSES = 4;  // member size classes of the tile-policy auto
 struct GroupTensor {
   const unsigned char* in;
   unsigned char* out;
-  const int* ldOff;
-  const int* stOff;
-  const unsigned short* stSm;
+  const int* ldRow;  // [tileVol / inRun]  input offset of each input run
+  const int* stRow;  // [tileVol / outRun] output offset of each output run
+  const int* smRow;  // [tileVol / outRun] in-tile index of each output run's first element
+  const int* smRun;  // [outRun] in-tile index of each element of an output run, from the first
   uint32_t firstTile;  // index of this tensor's first tile in the bucket
-  int nIn, nOut;
+  int nIn, nOut;       // load / store units of a tile
+  FastDiv inRun, outRun;
   int padShift, padLog;
   int nGR;
   FastDiv grDiv[GROUP_MAXG];
@@ -40,20 +45,23 @@ struct GroupTensor {
   long long grLastIn[GROUP_MAXG], grLastOut[GROUP_MAXG];
 };
 
-// Offset-table job for one member (written once, at group creation).
+// Run-table job for one member (written once, at group creation).
 struct GroupTableJob {
   TileParams tp;
-  int* ldOff;
-  int* stOff;
-  unsigned short* stSm;
+  GroupRunSplit rs;
+  int* ldRow;
+  int* stRow;
+  int* smRow;
+  int* smRun;
 };
 
-// Launch of one bucket's kernel (defined per element size in k_tile*.cu).
-cudaError_t launchGroupTile4(int lv, int sv, int nl, const GroupTensor* tens,
+// Launch of one bucket's kernel (defined per element size in k_tile*.cu);
+// async: loads by cp.async instead of through registers.
+cudaError_t launchGroupTile4(int lv, int sv, int nl, bool async, const GroupTensor* tens,
                              const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
-cudaError_t launchGroupTile8(int lv, int sv, int nl, const GroupTensor* tens,
+cudaError_t launchGroupTile8(int lv, int sv, int nl, bool async, const GroupTensor* tens,
                              const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
-cudaError_t launchGroupTile16(int lv, int sv, int nl, const GroupTensor* tens,
+cudaError_t launchGroupTile16(int lv, int sv, int nl, bool async, const GroupTensor* tens,
                               const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
 
 }  // namespace lt

@@ -186,6 +186,7 @@ cudaError_t launchPlan(const PlanDesc& pd, const DeviceTables* dt, const void* i
       if ((pd.tile.lv > 1 || pd.tile.sv > 1) && align % 16 != 0) {
         // 16-byte units need 16-byte aligned tensors; fall back to element
         // units and the persistent pipeline, which builds its own tables
+        if (pd.tileScalar.tileVol == 0) return cudaErrorInvalidValue;  // not finalized
         scalar = pd;
         scalar.tile = pd.tileScalar;
         scalar.slots = pd.slotsScalar;

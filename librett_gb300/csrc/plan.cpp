@@ -245,6 +245,54 @@ void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short
   }
 }
 
+GroupRunSplit groupRunSplit(const TileParams& tp) {
+  GroupRunSplit rs;
+  int k = 0;
+  long long run = 1;
+  while (k < tp.nTR && tp.trSin[k] == run) run *= tp.trE[k++];
+  rs.inRun = (int)run;
+  rs.kIn = k;
+  k = 0;
+  run = 1;
+  while (k < tp.nTR && tp.trSout[tp.trOut[k]] == run) run *= tp.trE[tp.trOut[k++]];
+  rs.outRun = (int)run;
+  rs.kOut = k;
+  return rs;
+}
+
+void groupRunTablesHost(const TileParams& tp, const GroupRunSplit& rs, int* ldRow, int* stRow,
+                        int* smRow, int* smRun) {
+  for (int r = 0; r < tp.tileVol / rs.inRun; ++r) {
+    int rem = r, off = 0;
+    for (int t = rs.kIn; t < tp.nTR; ++t) {
+      off += (rem % tp.trE[t]) * tp.trSin[t];
+      rem /= tp.trE[t];
+    }
+    ldRow[r] = off;
+  }
+  for (int r = 0; r < tp.tileVol / rs.outRun; ++r) {
+    int rem = r, off = 0, jj = 0;
+    for (int i = rs.kOut; i < tp.nTR; ++i) {
+      const int t = tp.trOut[i];
+      const int c = rem % tp.trE[t];
+      rem /= tp.trE[t];
+      off += c * tp.trSout[t];
+      jj += c * tp.trInTile[t];
+    }
+    stRow[r] = off;
+    smRow[r] = jj;
+  }
+  for (int a = 0; a < rs.outRun; ++a) {
+    int rem = a, jj = 0;
+    for (int i = 0; i < rs.kOut; ++i) {
+      const int t = tp.trOut[i];
+      jj += (rem % tp.trE[t]) * tp.trInTile[t];
+      rem /= tp.trE[t];
+    }
+    smRun[a] = jj;
+  }
+}
+
 namespace {
 
 // Wavefronts of 32-lane accesses: phases of 128 bytes; per phase the largest

@@ -189,6 +189,24 @@ bool finalizePlan(PlanDesc& pd);
 // tile_kernel.cuh): ldOff[nIn], stOff[nOut], stSm[tileVol].
 void tileTablesHost(const TileParams& tp, int* ldOff, int* stOff, unsigned short* stSm);
 
+// Run split of a tile (grouped execution).  The tile's elements in input
+// order form contiguous input runs of inRun elements (the leading tile ranks
+// whose input strides continue the previous ranks' extents), and in output
+// order contiguous output runs of outRun elements; a unit's offsets are then
+// a per-run table entry plus its position inside the run.
+struct GroupRunSplit {
+  int inRun, outRun;  // elements per input / output run
+  int kIn, kOut;      // tile ranks (input / output order) inside one run
+};
+GroupRunSplit groupRunSplit(const TileParams& tp);
+
+// Host copy of the run tables: ldRow[tileVol / inRun] input offset of each
+// input run; stRow / smRow[tileVol / outRun] output offset and in-tile
+// (input-order) index of each output run's first element; smRun[outRun]
+// in-tile index of each element of an output run relative to its first.
+void groupRunTablesHost(const TileParams& tp, const GroupRunSplit& rs, int* ldRow, int* stRow,
+                        int* smRow, int* smRun);
+
 // Shared-memory bank wavefronts of the first sampleUnits load and store
 // units of a tile for a given padding.
 long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits);

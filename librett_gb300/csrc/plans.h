@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <memory>
+#include <mutex>
 #include <string>
 
 #include "launch.h"
@@ -22,6 +23,19 @@ struct PlanObj {
   int lastGrid = 0;
   void* tablesAlloc = nullptr;  // device tables of flat-pipeline plans
   DeviceTables tables;
+  // The element-unit geometry (pd.tileScalar), built on the first launch
+  // with pointers that are not 16-byte aligned.
+  std::once_flag scalarOnce;
+  bool scalarOk = false;
+  bool ensureScalar() {
+    std::call_once(scalarOnce, [this] { scalarOk = finalizePlan(pd); });
+    return scalarOk;
+  }
+  // Whether a launch with these pointers uses the element-unit geometry.
+  bool needsScalar(const void* in, const void* out) const {
+    return pd.kernel == K_TILE && (pd.tile.lv > 1 || pd.tile.sv > 1) &&
+           (((uintptr_t)in | (uintptr_t)out) % 16) != 0;
+  }
   PlanObj() = default;
   PlanObj(const PlanObj&) = delete;
   PlanObj& operator=(const PlanObj&) = delete;

@@ -55,6 +55,21 @@ __device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
 }
 
+// cp.async of one 4-, 8- or 16-byte unit (16 bytes bypass L1).
+template <int BYTES>
+__device__ __forceinline__ void cpAsyncUnit(uint32_t dst, const void* src) {
+  static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async unit");
+  if constexpr (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cpAsyncWaitAll() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 __device__ __forceinline__ void cpAsyncCommit() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
 }
@@ -291,9 +306,14 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 }
 
 // Grouped flat kernel: CTA b moves one tile of tensor tileTensor[b] of a
-// bucket; the tensor's descriptor gives its pointers, offset tables and the
-// decode of its local tile index (same arithmetic as decodeTile).
-template <int ES, int LV, int SV, int NL>
+// bucket; the tensor's descriptor gives its pointers, run tables and the
+// decode of its local tile index (same arithmetic as decodeTile).  Unit
+// offsets come from the run split (GroupTensor): a small table entry per
+// run plus the position inside the run, so the tables stay in L1 even when
+// consecutive CTAs belong to different tensors.  ASYNC loads the units with
+// cp.async straight into shared memory (no data registers, so more CTAs fit
+// an SM) instead of staging them in registers.
+template <int ES, int LV, int SV, int NL, bool ASYNC>
 __global__ void __launch_bounds__(TILE_THREADS)
 groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ tileTensor) {
   using T = typename Word<ES>::T;
@@ -320,42 +340,67 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ ti
   }
   const T* in = reinterpret_cast<const T*>(g->in) + bin;
   T* out = reinterpret_cast<T*>(g->out) + bout;
-  const int* ldOff = g->ldOff;
+  const int* ldRow = g->ldRow;
+  const FastDiv inRun = g->inRun;
   const int nIn = g->nIn, nOut = g->nOut, padShift = g->padShift, padLog = g->padLog;
-  LT v[NL];
+  auto pad = [&](int j) { return j + ((j >> padShift) << padLog); };
+  if constexpr (ASYNC) {
+    const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
 #pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    const int u = threadIdx.x + k * TILE_THREADS;
-    if (u < nIn) v[k] = *reinterpret_cast<const LT*>(in + __ldg(ldOff + u));
-  }
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < nIn) {
+        const int j = u * LV;
+        const uint32_t r = fdiv((uint32_t)j, inRun);
+        const int a = j - (int)(r * inRun.d);
+        cpAsyncUnit<ES * LV>(sBase + (uint32_t)pad(j) * ES, in + a + __ldg(ldRow + r));
+      }
+    }
+    cpAsyncWaitAll();
+  } else {
+    LT v[NL];
 #pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    const int u = threadIdx.x + k * TILE_THREADS;
-    if (u < nIn) {
-      const int j = u * LV;
-      *reinterpret_cast<LT*>(s + j + ((j >> padShift) << padLog)) = v[k];
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < nIn) {
+        const int j = u * LV;
+        const uint32_t r = fdiv((uint32_t)j, inRun);
+        const int a = j - (int)(r * inRun.d);
+        v[k] = *reinterpret_cast<const LT*>(in + a + __ldg(ldRow + r));
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < nIn) *reinterpret_cast<LT*>(s + pad(u * LV)) = v[k];
     }
   }
   __syncthreads();
-  const int* stOff = g->stOff;
-  const unsigned short* stSm = g->stSm;
+  const int* stRow = g->stRow;
+  const int* smRow = g->smRow;
+  const int* smRun = g->smRun;
+  const FastDiv outRun = g->outRun;
 #pragma unroll 4
   for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
-    T* dst = out + __ldg(stOff + w);
+    const int q = w * SV;
+    const uint32_t r = fdiv((uint32_t)q, outRun);
+    const int a = q - (int)(r * outRun.d);
+    T* dst = out + a + __ldg(stRow + r);
+    const int jb = __ldg(smRow + r);
     if constexpr (SV == 1) {
-      *dst = s[__ldg(stSm + w)];
+      *dst = s[pad(jb + __ldg(smRun + a))];
     } else {
       T e[SV];
       if constexpr (SV == 2) {
-        const unsigned idx = __ldg(reinterpret_cast<const unsigned*>(stSm + 2 * w));
-        e[0] = s[idx & 0xffffu];
-        e[1] = s[idx >> 16];
+        const int2 jr = __ldg(reinterpret_cast<const int2*>(smRun + a));
+        e[0] = s[pad(jb + jr.x)];
+        e[1] = s[pad(jb + jr.y)];
       } else {
-        const uint2 idx = __ldg(reinterpret_cast<const uint2*>(stSm + 4 * w));
-        e[0] = s[idx.x & 0xffffu];
-        e[1] = s[idx.x >> 16];
-        e[2] = s[idx.y & 0xffffu];
-        e[3] = s[idx.y >> 16];
+        const int4 jr = __ldg(reinterpret_cast<const int4*>(smRun + a));
+        e[0] = s[pad(jb + jr.x)];
+        e[1] = s[pad(jb + jr.y)];
+        e[2] = s[pad(jb + jr.z)];
+        e[3] = s[pad(jb + jr.w)];
       }
       ST val;
       __builtin_memcpy(&val, e, sizeof(ST));

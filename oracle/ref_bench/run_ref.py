@@ -10,7 +10,9 @@ oracle/_ref/ref_driver with nvcc for sm_103a, then:
   --bench  : times LibreTT on the small case, the two small-leading-dimension
              cases and the first --suite problems of the random-shape suite;
   --loop N : times LibreTT's per-tensor librettExecute loop over N problems of
-             the batched distribution (librett_gb300.workloads).
+             the batched distribution (librett_gb300.workloads);
+  --planning N : times LibreTT's librettPlan and librettPlanMeasure on N
+             problems of the plan-selection distribution.
 
 Usage: python oracle/ref_bench/run_ref.py --src <LibreTT src dir> --out <dir>
        [--golden] [--bench] [--suite N] [--measure]
@@ -89,6 +91,25 @@ def run_bench(out: Path, nsuite: int, measure: bool, steps: int = 10, warmup: in
     return lines
 
 
+def run_planning(out: Path, n: int, seed: int):
+    """LibreTT's librettPlan and librettPlanMeasure latency on n problems of
+    the plan-selection distribution (librett_gb300.learn.data.problems)."""
+    sys.path.insert(0, str(ROOT))
+    from librett_gb300.learn.data import problems
+
+    cases = [(d, p, es, "none") for d, p, es in problems(n, seed)]
+    cf = out / "planning_cases.txt"
+    write_cases(cf, cases)
+    res = {}
+    for measure in (0, 1):
+        r = subprocess.run([str(DRIVER), "bench", str(cf), "1", "0", str(measure)], check=True,
+                           capture_output=True, text=True)
+        res["measure" if measure else "plan"] = [json.loads(x) for x in r.stdout.splitlines()
+                                                 if x.startswith("{")]
+    (out / "reference_planning.json").write_text(json.dumps(res) + "\n")
+    return res
+
+
 def run_loop(out: Path, n: int, steps: int = 5, warmup: int = 3):
     sys.path.insert(0, str(ROOT))
     from librett_gb300.workloads import grouped_problems
@@ -111,6 +132,10 @@ def main(argv=None):
     ap.add_argument("--bench", action="store_true")
     ap.add_argument("--measure", action="store_true", help="bench with librettPlanMeasure")
     ap.add_argument("--suite", type=int, default=40)
+    ap.add_argument("--planning", type=int, default=0,
+                    help="time LibreTT's librettPlan and librettPlanMeasure on this many problems "
+                         "of the plan-selection distribution")
+    ap.add_argument("--planning-seed", type=int, default=424242)
     ap.add_argument("--loop", type=int, default=0,
                     help="time LibreTT's per-tensor librettExecute loop over this many "
                          "problems of the batched distribution")
@@ -127,6 +152,12 @@ def main(argv=None):
         if args.measure:
             lines = run_bench(out, args.suite, True)
             print(f"bench (plan measure): {len(lines)} cases timed")
+    if args.planning:
+        res = run_planning(out, args.planning, args.planning_seed)
+        import statistics
+        print("planning: median plan_ms librettPlan %.3f, librettPlanMeasure %.3f" % (
+            statistics.median(x["plan_ms"] for x in res["plan"]),
+            statistics.median(x["plan_ms"] for x in res["measure"])))
     if args.loop:
         line = run_loop(out, args.loop)
         print("loop: " + json.dumps(line))

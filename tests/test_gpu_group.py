@@ -134,7 +134,8 @@ def test_group_separate_member(cuda):
 
 
 @pytest.mark.parametrize("policy", [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2), (3, 3, 3, 3),
-                                    (2, 0, 3, 1)])
+                                    (4, 4, 4, 4), (5, 5, 5, 5), (6, 6, 6, 6), (7, 7, 7, 7),
+                                    (2, 4, 3, 5), (6, 0, 7, 1)])
 def test_group_policies(cuda, policy):
     import torch
 
@@ -164,7 +165,7 @@ def test_group_tune_and_cache(cuda):
     with L.Group(plans, ins, outs, stream) as g:
         g.tune()
         pol, tuned = g.policy()
-        assert tuned and all(0 <= x < 4 for x in pol)
+        assert tuned and all(0 <= x < 8 for x in pol)
         b.out.fill_(CANARY)
         g.execute()
         b.check()
@@ -266,5 +267,5 @@ def test_group_errors(cuda):
     assert lib.librett_c_group_tune(987654) == L.LIBRETT_INVALID_PLAN
     with L.Plan([8, 16], [1, 0], 4, s) as p:
         with pytest.raises(L.LibrettError) as e:
-            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 7, 0))
+            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 8, 0))
         assert e.value.code == L.LIBRETT_INVALID_PARAMETER
