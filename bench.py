@@ -637,10 +637,12 @@ def run_grouped(args):
         "untuned": {"ms_per_step": round(untuned_ms, 4),
                     "transposes_per_s": round(world * n / (untuned_ms / 1e3), 1),
                     "gbs": round(step_bytes / (untuned_ms / 1e3) / 1e9, 3)},
-        "tile_policy": {"per_size_class": policy, "tuned": tuned,
+        "tile_policy": {"per_class": policy, "tuned": tuned,
                         "tune_s": None if tune_s is None else round(tune_s, 3),
-                        "classes": "<64KiB, <1MiB, <16MiB, larger",
-                        "values": "0 selector, 1 wide, 2 widest, 3 full-device model"},
+                        "classes": "size class (<64KiB, <1MiB, <16MiB, larger) + 4 x element "
+                                   "size (4, 8, 16 bytes)",
+                        "values": "tile (0 selector, 1 wide, 2 widest, 3 full-device model) + 4 x "
+                                  "loads (0 registers, 1 cp.async, 2 aligned run reads)"},
         "plan_s": round(plan_s, 3),
         "group_create_s": round(create_s, 3),
         "roofline": {"bound": "hbm", "kernel": "groupTileKernel", "achieved": round(gbs, 3),
@@ -673,7 +675,8 @@ def main(argv=None):
     ap.add_argument("--buckets", type=str, default=None,
                     help="grouped workload: write the graph's bucket launches (JSON lines)")
     ap.add_argument("--policy", type=str, default=None,
-                    help="grouped workload: tile policy per size class, e.g. 0,1,1,0 (no tuning)")
+                    help="grouped workload: policy for all classes, per size class (4 values) or per "
+                         "class (12 values), e.g. 6 or 0,1,1,0 (no tuning)")
     ap.add_argument("--no-tune", action="store_true",
                     help="grouped workload: keep the plan selector's tiles (no autotuning)")
     ap.add_argument("--dims", type=str, default=None, help="custom problem: comma-separated dims")

@@ -113,6 +113,15 @@ int librett_c_transpose_noalloc(int rank, const int* dim, const int* permutation
                                 size_t sizeofType, void* stream, const void* idata,
                                 void* odata);
 
+/* Device-side verifier (the role of LibreTT's device checker,
+ * src/TensorTester.cpp:47-126): compares every element of odata with the
+ * element of idata the transpose formula names, on the device, and returns
+ * the number of mismatching elements and the smallest mismatching output
+ * index (-1 if none).  Synchronises `stream`.  Fused dims must be < 2^31. */
+int librett_c_verify(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                     const void* idata, const void* odata, void* stream,
+                     unsigned long long* mismatches, long long* first_bad);
+
 /* ---- Learned plan selection (no LibreTT counterpart; replaces the role of
  * LibreTT's analytic GpuModel ranking, src/plan.cpp:1073-1643) ---- */
 
@@ -133,6 +142,15 @@ int librett_c_set_plan_selector(int mode);
  * LIBRETT_ALL_PIPELINES=1 environment variable sets 1).  Returns the
  * previous setting.  Changes candidate numbering. */
 int librett_c_set_candidate_set(int all);
+
+/* Plan cache (no LibreTT counterpart): librett_c_plan / librettPlan reuse
+ * the planner's choice for a fused problem already planned on this device.
+ * Sets the capacity in entries (0 disables; the LIBRETT_PLAN_CACHE
+ * environment variable sets the initial value, default 4096) and returns the
+ * previous one.  Changing the selector, its model or the candidate set
+ * clears the cache. */
+int librett_c_set_plan_cache(int capacity);
+int librett_c_plan_cache_stats(long long* hits, long long* misses, int* entries);
 
 /* Load a weight file (NULL: the default, LIBRETT_PLAN_MODEL or
  * models/plan_mlp.bin next to the library).  A missing, truncated,
@@ -164,23 +182,26 @@ typedef unsigned int librettGroupHandle;
 #endif
 int librett_c_group_create(librettGroupHandle* group, int count, const librettHandle* plans,
                            void* const* idata, void* const* odata, void* stream);
-/* As librett_c_group_create with the policy given per member size class
- * (policy[4]: classes < 64 KiB, < 1 MiB, < 16 MiB, larger).  A policy is
+/* As librett_c_group_create with the policy given per member class
+ * (policy[12]: class = size class + 4 * element-size index; size classes
+ * < 64 KiB, < 1 MiB, < 16 MiB, larger; element sizes 4, 8, 16).  A policy is
  * tile + 4 * loads: tile 0 = plan selector's tile, 1 = largest tile within
  * 10% of the best sector efficiency, 2 = largest tile, 3 = analytic model for
  * a full device; loads 0 = through registers, 1 = cp.async into shared
- * memory.  Values 0..7. */
+ * memory, 2 = aligned 16-byte reads of each input run scattered into shared
+ * memory (element-size load units narrower than 16 bytes; others use 1).
+ * Values 0..11. */
 int librett_c_group_create_policy(librettGroupHandle* group, int count,
                                   const librettHandle* plans, void* const* idata,
                                   void* const* odata, void* stream, const int* policy);
 int librett_c_group_tune(librettGroupHandle group);
 /* Bucket `index` (launch order) of the group's graph: shape[6] = element
  * bytes, load unit, store unit (elements), load units per thread, dynamic
- * shared memory bytes, cp.async loads (0/1); its members, tiles and
- * algorithmic bytes. */
+ * shared memory bytes, loads (0/1/2 as in the policy); its members, tiles
+ * and algorithmic bytes. */
 int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int* members,
                            long long* tiles, long long* bytes);
-/* policy[4] in use, and whether it came from tuning (this group's or a
+/* policy[12] in use, and whether it came from tuning (this group's or a
  * cached one for the same batch signature). */
 int librett_c_group_policy(librettGroupHandle group, int* policy, int* tuned);
 int librett_c_group_execute(librettGroupHandle group);

@@ -129,7 +129,7 @@ class Group:
 
     # policies per member size class (librett_c.h): tile + 4 * loads
     POLICY_SELECTOR, POLICY_WIDE, POLICY_WIDEST, POLICY_FILL = 0, 1, 2, 3
-    LOADS_REGISTERS, LOADS_ASYNC = 0, 4
+    LOADS_REGISTERS, LOADS_ASYNC, LOADS_RUNS = 0, 4, 8
 
     def __init__(self, plans, idata, odata, stream=None, *, policy=None):
         n, hs, ins, outs = _handle_arrays(plans, idata, odata)
@@ -138,7 +138,7 @@ class Group:
         if policy is None:
             rc = lib.librett_c_group_create(ctypes.byref(h), n, hs, ins, outs, _stream(stream))
         else:
-            pol = (ctypes.c_int * 4)(*[int(x) for x in policy])
+            pol = (ctypes.c_int * 12)(*expand_policy(policy))
             rc = lib.librett_c_group_create_policy(ctypes.byref(h), n, hs, ins, outs,
                                                    _stream(stream), pol)
         if rc != LIBRETT_SUCCESS:
@@ -163,12 +163,12 @@ class Group:
             if rc != LIBRETT_SUCCESS:
                 raise LibrettError(rc, "librett_c_group_bucket")
             out.append({"es": shape[0], "lv": shape[1], "sv": shape[2], "nl": shape[3],
-                        "smem": shape[4], "async": shape[5], "members": m.value, "tiles": t.value,
+                        "smem": shape[4], "loads": shape[5], "members": m.value, "tiles": t.value,
                         "bytes": by.value})
         return out
 
     def policy(self) -> tuple[list[int], bool]:
-        pol = (ctypes.c_int * 4)()
+        pol = (ctypes.c_int * 12)()
         tuned = ctypes.c_int(0)
         rc = _lib.load().librett_c_group_policy(self.handle, pol, ctypes.byref(tuned))
         if rc != LIBRETT_SUCCESS:
@@ -208,6 +208,20 @@ class Group:
             pass
 
 
+def expand_policy(policy) -> list[int]:
+    """A group policy per member class (12 values: size class + 4 * element-size
+    index) from 1 value (all classes), 4 values (per size class, every element
+    size) or 12 values."""
+    p = [int(x) for x in (policy if hasattr(policy, "__len__") else [policy])]
+    if len(p) == 1:
+        return p * 12
+    if len(p) == 4:
+        return p * 3
+    if len(p) == 12:
+        return p
+    raise ValueError("a group policy has 1, 4 or 12 values")
+
+
 def _handle_arrays(plans, idata, odata):
     n = len(plans)
     if len(idata) != n or len(odata) != n:
@@ -232,6 +246,18 @@ def execute_batch(plans, idata, odata) -> None:
     rc = _lib.load().librett_c_execute_batch(n, hs, ins, outs)
     if rc != LIBRETT_SUCCESS:
         raise LibrettError(rc, "librett_c_execute_batch")
+
+
+def verify(dim, permutation, sizeofType: int, idata: int, odata: int, stream=None):
+    """Device-side check of a transpose (librett_c_verify): returns (number of
+    mismatching output elements, smallest mismatching output index or -1)."""
+    bad, first = ctypes.c_ulonglong(0), ctypes.c_longlong(-1)
+    rc = _lib.load().librett_c_verify(len(dim), _lib.int_array(dim), _lib.int_array(permutation),
+                                      sizeofType, ctypes.c_void_p(idata), ctypes.c_void_p(odata),
+                                      _stream(stream), ctypes.byref(bad), ctypes.byref(first))
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_verify")
+    return bad.value, first.value
 
 
 def launch_count() -> int:

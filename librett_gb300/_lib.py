@@ -97,6 +97,10 @@ C_FUNCTIONS = [
       ctypes.POINTER(ctypes.c_float), ctypes.c_int]),
     ("librett_c_set_candidate_set", ctypes.c_int, [ctypes.c_int]),
     ("librett_c_set_plan_selector", ctypes.c_int, [ctypes.c_int]),
+    ("librett_c_set_plan_cache", ctypes.c_int, [ctypes.c_int]),
+    ("librett_c_plan_cache_stats", ctypes.c_int,
+     [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+      ctypes.POINTER(ctypes.c_int)]),
     ("librett_c_load_plan_model", ctypes.c_int, [ctypes.c_char_p]),
     ("librett_c_mlp_param_count", ctypes.c_int, []),
     ("librett_c_mlp_feature_count", ctypes.c_int, []),
@@ -126,6 +130,9 @@ C_FUNCTIONS = [
     ("librett_c_group_destroy", ctypes.c_int, [_H]),
     ("librett_c_execute_grouped", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    ("librett_c_verify", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
+      _P, _P, _P, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_group_run_check", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
       ctypes.c_int, ctypes.c_int, ctypes.c_int]),

@@ -24,7 +24,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "librett.so"
 
 SOURCES = ["api.cpp", "plan.cpp", "select.cpp", "k_misc.cu", "k_tile4.cu", "k_tile8.cu",
-           "k_tile16.cu", "noalloc.cu", "mlp.cu", "group.cu"]
+           "k_tile16.cu", "noalloc.cu", "mlp.cu", "group.cu", "verify.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           f"-I{INCLUDE}", f"-I{CSRC}"]

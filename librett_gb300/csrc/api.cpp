@@ -8,7 +8,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
+#include <list>
 #include <memory>
 #include <mutex>
 #include <shared_mutex>
@@ -147,6 +149,50 @@ librettResult activate(librettHandle* handle, const lt::PlanDesc& pd, cudaStream
 
 // Shared by librettPlan and librett_c_plan_candidate: plan with the given
 // candidate (or the heuristic's choice when candidate < 0).
+// Plan cache: the planner's choice per (device, fused problem), so that a
+// repeated shape skips candidate enumeration and selection (LibreTT re-plans
+// every call; its launch-configuration LRU, src/kernel.cpp:671-691, caches
+// only occupancy).  Least recently used entries are evicted beyond the
+// capacity (LIBRETT_PLAN_CACHE entries, default 4096; 0 disables).  Cleared
+// whenever the selector, its model or the candidate set changes.
+struct CachedPlan {
+  lt::PlanDesc pd;
+  int selectedBy;
+};
+std::mutex gCacheMu;
+std::list<std::pair<std::string, CachedPlan>> gCacheLru;  // most recent first
+std::unordered_map<std::string, std::list<std::pair<std::string, CachedPlan>>::iterator> gCache;
+int gCacheCap = -1;
+long long gCacheHits = 0, gCacheMisses = 0;
+
+int cacheCapacityLocked() {
+  if (gCacheCap < 0) {
+    const char* e = std::getenv("LIBRETT_PLAN_CACHE");
+    gCacheCap = e != nullptr && *e ? std::max(0, std::atoi(e)) : 4096;
+  }
+  return gCacheCap;
+}
+
+void cacheClear() {
+  std::lock_guard<std::mutex> lk(gCacheMu);
+  gCache.clear();
+  gCacheLru.clear();
+}
+
+std::string cacheKey(const lt::Fused& f, int dev, int sms) {
+  std::string k;
+  auto put = [&](long long v) { k.append(reinterpret_cast<const char*>(&v), sizeof(v)); };
+  put(dev);
+  put(sms);
+  put(f.rank);
+  put(f.esize);
+  for (int r = 0; r < f.rank; ++r) {
+    put(f.dim[r]);
+    put(f.perm[r]);
+  }
+  return k;
+}
+
 librettResult planImpl(librettHandle* handle, int rank, const int* dim, const int* perm,
                        size_t sizeofType, cudaStream_t stream, int candidate) {
   if (handle == nullptr) return LIBRETT_INVALID_PARAMETER;
@@ -156,12 +202,41 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   if (!currentDevice(dev, sms, &devName)) return LIBRETT_INTERNAL_ERROR;
   lt::Fused f;
   lt::fuseRanks(rank, dim, perm, (int)sizeofType, f);
+  std::string key;
+  if (candidate < 0) {
+    key = cacheKey(f, dev, sms);
+    std::unique_lock<std::mutex> lk(gCacheMu);
+    if (cacheCapacityLocked() > 0) {
+      auto it = gCache.find(key);
+      if (it != gCache.end()) {
+        gCacheLru.splice(gCacheLru.begin(), gCacheLru, it->second);
+        ++gCacheHits;
+        const CachedPlan hit = it->second->second;
+        lk.unlock();
+        return activate(handle, hit.pd, stream, dev, sms, hit.selectedBy);
+      }
+      ++gCacheMisses;
+    }
+  }
   std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   bool learned = false;
   int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName.c_str(), &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
-  return activate(handle, cands[pick], stream, dev, sms, candidate >= 0 ? 3 : (learned ? 1 : 0));
+  const int selectedBy = candidate >= 0 ? 3 : (learned ? 1 : 0);
+  if (candidate < 0) {
+    std::lock_guard<std::mutex> lk(gCacheMu);
+    const int cap = cacheCapacityLocked();
+    if (cap > 0 && gCache.find(key) == gCache.end()) {
+      gCacheLru.emplace_front(key, CachedPlan{cands[pick], selectedBy});
+      gCache[key] = gCacheLru.begin();
+      while ((int)gCacheLru.size() > cap) {
+        gCache.erase(gCacheLru.back().first);
+        gCacheLru.pop_back();
+      }
+    }
+  }
+  return activate(handle, cands[pick], stream, dev, sms, selectedBy);
 }
 
 }  // namespace
@@ -394,6 +469,7 @@ int librett_c_candidate_features(int rank, const int* dim, const int* permutatio
 int librett_c_set_candidate_set(int all) {
   const int prev = lt::allPipelines() ? 1 : 0;
   lt::setAllPipelines(all != 0);
+  cacheClear();
   return prev;
 }
 
@@ -401,12 +477,34 @@ int librett_c_set_plan_selector(int mode) {
   if (mode < 0 || mode > 2) return -1;
   const int prev = lt::selectorMode();
   lt::setSelectorMode(mode);
+  cacheClear();
   return prev;
 }
 
 int librett_c_load_plan_model(const char* path) {
   std::string why;
-  return lt::loadSelectorModel(path, &why) ? LIBRETT_SUCCESS : LIBRETT_INVALID_PARAMETER;
+  const bool ok = lt::loadSelectorModel(path, &why);
+  cacheClear();
+  return ok ? LIBRETT_SUCCESS : LIBRETT_INVALID_PARAMETER;
+}
+
+int librett_c_set_plan_cache(int capacity) {
+  std::lock_guard<std::mutex> lk(gCacheMu);
+  const int prev = cacheCapacityLocked();
+  gCacheCap = std::max(0, capacity);
+  while ((int)gCacheLru.size() > gCacheCap) {
+    gCache.erase(gCacheLru.back().first);
+    gCacheLru.pop_back();
+  }
+  return prev;
+}
+
+int librett_c_plan_cache_stats(long long* hits, long long* misses, int* entries) {
+  std::lock_guard<std::mutex> lk(gCacheMu);
+  if (hits) *hits = gCacheHits;
+  if (misses) *misses = gCacheMisses;
+  if (entries) *entries = (int)gCacheLru.size();
+  return LIBRETT_SUCCESS;
 }
 
 int librett_c_mlp_predict_host(const float* params, const float* x, int n, float* out) {

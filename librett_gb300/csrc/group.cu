@@ -84,20 +84,23 @@ size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[4
 
 // Policies: policy % GP_TILES picks a member's flat tile from its
 // candidates; policy / GP_TILES picks the bucket's loads (0 registers,
-// 1 cp.async).
+// 1 cp.async, 2 aligned 16-byte run reads where the load units are narrower
+// than 16 bytes, else cp.async).
 enum GroupPolicy {
   GP_SELECTOR = 0,  // the plan selector's choice for the tensor on its own
   GP_WIDE = 1,      // the largest tile within 10% of the best sector efficiency
   GP_WIDEST = 2,    // the largest tile
   GP_FILL = 3,      // the analytic model with the device assumed full of other work
   GP_TILES = 4,
-  GP_COUNT = 2 * GP_TILES
+  GP_COUNT = 3 * GP_TILES
 };
 constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
 
-// Member size classes (bytes of one tensor): < 64 KiB, < 1 MiB, < 16 MiB, larger.
-int sizeClass(long long bytes) {
-  return bytes < (1LL << 16) ? 0 : bytes < (1LL << 20) ? 1 : bytes < (1LL << 24) ? 2 : 3;
+// Member class: size class (bytes of one tensor < 64 KiB, < 1 MiB, < 16 MiB,
+// larger) + 4 * element-size index (4, 8, 16 bytes).
+int memberClass(long long bytes, int esize) {
+  const int sc = bytes < (1LL << 16) ? 0 : bytes < (1LL << 20) ? 1 : bytes < (1LL << 24) ? 2 : 3;
+  return sc + 4 * (esize == 4 ? 0 : esize == 8 ? 1 : 2);
 }
 
 using Policy = std::array<int, GROUP_CLASSES>;
@@ -114,7 +117,7 @@ struct Member {
 };
 
 struct BucketSummary {
-  int es, lv, sv, nl, async, members, smem;
+  int es, lv, sv, nl, loads, members, smem;
   long long tiles, bytes;
 };
 
@@ -181,12 +184,12 @@ uint64_t fnv(uint64_t h, uint64_t v) {
   return h;
 }
 
-cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, bool async, const GroupTensor* tens,
+cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, int loads, const GroupTensor* tens,
                               const int* map, uint32_t tiles, int smem, cudaStream_t s) {
   switch (es) {
-    case 4: return launchGroupTile4(lv, sv, nl, async, tens, map, tiles, smem, s);
-    case 8: return launchGroupTile8(lv, sv, nl, async, tens, map, tiles, smem, s);
-    case 16: return launchGroupTile16(lv, sv, nl, async, tens, map, tiles, smem, s);
+    case 4: return launchGroupTile4(lv, sv, nl, loads, tens, map, tiles, smem, s);
+    case 8: return launchGroupTile8(lv, sv, nl, loads, tens, map, tiles, smem, s);
+    case 16: return launchGroupTile16(lv, sv, nl, loads, tens, map, tiles, smem, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -245,7 +248,7 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
 }
 
 struct Bucket {
-  int es, lv, sv, nl, async;
+  int es, lv, sv, nl, loads;
   int smem = 0;
   uint32_t tiles = 0;
   long long bytes = 0;
@@ -279,8 +282,9 @@ librettResult build(GroupObj& g, const Policy& pol) {
       continue;
     }
     const PlanDesc& pd = m.pd;
-    const int async = pol[m.cls] / GP_TILES;
-    auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots, async,
+    int loads = pol[m.cls] / GP_TILES;
+    if (loads == 2 && (pd.tile.lv > 1 || pd.f.esize == 16)) loads = 1;  // run reads need narrow units
+    auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots, loads,
                                (pd.smemBytes + SMEM_CLASS - 1) / SMEM_CLASS);
     auto it = key2b.find(key);
     if (it == key2b.end()) {
@@ -289,7 +293,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       b.lv = pd.tile.lv;
       b.sv = pd.tile.sv;
       b.nl = pd.slots;
-      b.async = async;
+      b.loads = loads;
       it = key2b.emplace(key, (int)buckets.size()).first;
       buckets.push_back(b);
     }
@@ -362,6 +366,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.nOut = tp.nOut;
       t.inRun = makeFastDiv((uint32_t)rs.inRun);
       t.outRun = makeFastDiv((uint32_t)rs.outRun);
+      t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
       t.nGR = tp.nGR;
@@ -432,9 +437,9 @@ librettResult build(GroupObj& g, const Policy& pol) {
       load[br] += nd.bytes;
       if (nd.bucket >= 0) {
         const Bucket& b = buckets[nd.bucket];
-        B.summary.push_back({b.es, b.lv, b.sv, b.nl, b.async, (int)b.members.size(), b.smem,
+        B.summary.push_back({b.es, b.lv, b.sv, b.nl, b.loads, (int)b.members.size(), b.smem,
                              (long long)b.tiles, b.bytes});
-        launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl, b.async != 0,
+        launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl, b.loads,
                                      reinterpret_cast<const GroupTensor*>(base + b.tensOff),
                                      reinterpret_cast<const int*>(base + b.mapOff), b.tiles,
                                      b.smem, side[br]) == cudaSuccess;
@@ -508,7 +513,7 @@ librettResult create(librettGroupHandle* handle, int count, const librettHandle*
       return LIBRETT_INVALID_PARAMETER;
     const long long bytes = f.vol * (long long)f.esize;
     g->bytes += 2 * bytes;
-    m.cls = sizeClass(bytes);
+    m.cls = memberClass(bytes, f.esize);
     m.aligned16 = (uintptr_t)m.in % 16 == 0 && (uintptr_t)m.out % 16 == 0;
   }
   g->signature = batchSignature(*g);
@@ -577,9 +582,9 @@ bool timeBuild(GroupObj& g, cudaEvent_t e0, cudaEvent_t e1, float* ms) {
   return true;
 }
 
-// Autotuner.  Phase 1 times every policy applied to all size classes and
-// keeps the fastest; phase 2 walks the classes that hold at least 2% of the
-// group's bytes (largest class first) and tries, for one class at a time,
+// Autotuner.  Phase 1 times every policy applied to all classes and keeps
+// the fastest; phase 2 walks the classes that hold at least 2% of the
+// group's bytes (most bytes first) and tries, for one class at a time,
 // the other tile choices with the same loads and the other loads with the
 // same tile, keeping a change that is at least 2% faster.  Times on the
 // group's own buffers (reads the inputs, overwrites the outputs); the result
@@ -617,7 +622,12 @@ librettResult tune(librettGroupHandle h) {
       cur = pol;
     }
   }
-  for (int c = GROUP_CLASSES - 1; c >= 0 && r == LIBRETT_SUCCESS; --c) {
+  int order[GROUP_CLASSES];
+  for (int c = 0; c < GROUP_CLASSES; ++c) order[c] = c;
+  std::stable_sort(order, order + GROUP_CLASSES,
+                   [&](int a, int b) { return classBytes[a] > classBytes[b]; });
+  for (int oc = 0; oc < GROUP_CLASSES && r == LIBRETT_SUCCESS; ++oc) {
+    const int c = order[oc];
     if (classBytes[c] * 50 < g.bytes) continue;
     const int tile = cur[c] % GP_TILES, loads = cur[c] / GP_TILES;
     std::vector<int> alts;
@@ -742,7 +752,7 @@ int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int*
     shape[2] = b.sv;
     shape[3] = b.nl;
     shape[4] = b.smem;
-    shape[5] = b.async;
+    shape[5] = b.loads;
   }
   if (members) *members = b.members;
   if (tiles) *tiles = b.tiles;

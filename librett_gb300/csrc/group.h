@@ -10,7 +10,8 @@
 // compact descriptor run with their own launch inside the same graph.
 //
 // Which flat tile a member gets, and whether its bucket loads through
-// registers or cp.async, is a policy per member size class; an autotuner
+// registers or cp.async, is a policy per member class (size and element
+// size); an autotuner
 // (librettGroupTune) times the policies on the group's own buffers and keeps
 // the fastest combination, cached by the batch's signature.  Buckets are
 // also split by shared-memory size (4 KiB classes), so that a CTA reserves
@@ -26,7 +27,10 @@
 namespace lt {
 
 constexpr int GROUP_MAXG = 8;     // grid ranks a compact descriptor holds
-constexpr int GROUP_CLASSES = 4;  // member size classes of the tile-policy autotuner
+// Member classes of the tile-policy autotuner: 4 size classes (bytes of one
+// tensor < 64 KiB, < 1 MiB, < 16 MiB, larger) x 3 element sizes (4, 8, 16);
+// class = size class + 4 * log2(element bytes / 4).
+constexpr int GROUP_CLASSES = 12;
 
 struct GroupTensor {
   const unsigned char* in;
@@ -38,6 +42,7 @@ struct GroupTensor {
   uint32_t firstTile;  // index of this tensor's first tile in the bucket
   int nIn, nOut;       // load / store units of a tile
   FastDiv inRun, outRun;
+  FastDiv inSlots;  // aligned 16-byte blocks reserved per input run (loads 2)
   int padShift, padLog;
   int nGR;
   FastDiv grDiv[GROUP_MAXG];
@@ -56,12 +61,13 @@ struct GroupTableJob {
 };
 
 // Launch of one bucket's kernel (defined per element size in k_tile*.cu);
-// async: loads by cp.async instead of through registers.
-cudaError_t launchGroupTile4(int lv, int sv, int nl, bool async, const GroupTensor* tens,
+// loads: 0 registers, 1 cp.async, 2 aligned 16-byte run reads (element-size
+// load units narrower than 16 bytes only).
+cudaError_t launchGroupTile4(int lv, int sv, int nl, int loads, const GroupTensor* tens,
                              const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
-cudaError_t launchGroupTile8(int lv, int sv, int nl, bool async, const GroupTensor* tens,
+cudaError_t launchGroupTile8(int lv, int sv, int nl, int loads, const GroupTensor* tens,
                              const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
-cudaError_t launchGroupTile16(int lv, int sv, int nl, bool async, const GroupTensor* tens,
+cudaError_t launchGroupTile16(int lv, int sv, int nl, int loads, const GroupTensor* tens,
                               const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
 
 }  // namespace lt

@@ -310,10 +310,15 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 // decode of its local tile index (same arithmetic as decodeTile).  Unit
 // offsets come from the run split (GroupTensor): a small table entry per
 // run plus the position inside the run, so the tables stay in L1 even when
-// consecutive CTAs belong to different tensors.  ASYNC loads the units with
-// cp.async straight into shared memory (no data registers, so more CTAs fit
-// an SM) instead of staging them in registers.
-template <int ES, int LV, int SV, int NL, bool ASYNC>
+// consecutive CTAs belong to different tensors.  LOADS: 0 stages the load
+// units in registers; 1 copies them with cp.async straight into shared
+// memory (no data registers, so more CTAs fit an SM); 2, for element-size
+// load units narrower than 16 bytes, reads each input run with aligned
+// 16-byte loads and scatters the run's elements into shared memory.  An
+// aligned 16-byte block that holds a byte of the tensor lies in the same
+// memory page as that byte, so these reads stay in mapped memory even where
+// the block extends past the tensor; the bytes outside the run are dropped.
+template <int ES, int LV, int SV, int NL, int LOADS>
 __global__ void __launch_bounds__(TILE_THREADS)
 groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ tileTensor) {
   using T = typename Word<ES>::T;
@@ -344,7 +349,31 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ ti
   const FastDiv inRun = g->inRun;
   const int nIn = g->nIn, nOut = g->nOut, padShift = g->padShift, padLog = g->padLog;
   auto pad = [&](int j) { return j + ((j >> padShift) << padLog); };
-  if constexpr (ASYNC) {
+  if constexpr (LOADS == 2 && LV == 1 && ES < 16) {
+    constexpr int CH = 16 / ES;  // elements per 16-byte block
+    const int R = (int)inRun.d;
+    const FastDiv slots = g->inSlots;  // blocks reserved per run
+    const int items = (nIn / R) * (int)slots.d;
+#pragma unroll 4
+    for (int w = threadIdx.x; w < items; w += TILE_THREADS) {
+      const uint32_t r = fdiv((uint32_t)w, slots);
+      const int c = w - (int)(r * slots.d);
+      const long long A = (long long)reinterpret_cast<uintptr_t>(in + __ldg(ldRow + r));
+      const long long blk = (A & ~15LL) + 16LL * c;
+      if (blk < A + (long long)R * ES) {
+        const uint4 val = __ldg(reinterpret_cast<const uint4*>(blk));
+        T e[CH];
+        __builtin_memcpy(e, &val, sizeof(val));
+        const int a0 = (int)((blk - A) / ES);
+        const int j0 = (int)r * R;
+#pragma unroll
+        for (int k = 0; k < CH; ++k) {
+          const int a = a0 + k;
+          if (a >= 0 && a < R) s[pad(j0 + a)] = e[k];
+        }
+      }
+    }
+  } else if constexpr (LOADS >= 1) {
     const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
 #pragma unroll
     for (int k = 0; k < NL; ++k) {

@@ -2,7 +2,8 @@
 
 For held-out problems of the selector's distribution (a seed not used in
 training): planning latency of librettPlan with the learned model and with
-the analytic model, and of librettPlanMeasure (which times every candidate);
+the analytic model (plan cache off), of librettPlanMeasure (which times
+every candidate), and of a repeated librettPlan served by the plan cache;
 and the measured execute time of the learned and the analytic choice.
 
 Usage (on a GPU):
@@ -53,6 +54,7 @@ def evaluate(probs):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     rows = []
     prev = lib.librett_c_set_plan_selector(0)
+    prev_cache = lib.librett_c_set_plan_cache(0)  # every latency below is a full planning
     try:
         for dims, perm, es in probs:
             r = {"dims": dims, "perm": perm, "es": es}
@@ -84,14 +86,26 @@ def evaluate(probs):
             plan = L.Plan(dims, perm, es, stream, measure=(a.data_ptr(), b.data_ptr()))
             r["exec_ms_measure"] = _time_exec(plan, a.data_ptr(), b.data_ptr(), stream, ev) * 1e3
             plan.destroy()
+            # a repeated shape with the plan cache on (the second call hits)
+            lib.librett_c_set_plan_selector(0)
+            lib.librett_c_set_plan_cache(16)
+            for k in range(2):
+                h = ctypes.c_uint(0)
+                t0 = time.perf_counter()
+                rc = lib.librett_c_plan(ctypes.byref(h), len(dims), dims_c, perm_c, es, sptr)
+                r["plan_ms_cached"] = (time.perf_counter() - t0) * 1e3
+                assert rc == 0
+                lib.librett_c_destroy(h.value)
+            lib.librett_c_set_plan_cache(0)
             rows.append(r)
     finally:
         lib.librett_c_set_plan_selector(prev)
+        lib.librett_c_set_plan_cache(prev_cache)
     g = lambda x: float(np.exp(np.mean(np.log(x))))  # noqa: E731
     summary = {
         "problems": len(rows),
         "plan_ms_median": {k: float(np.median([r[f"plan_ms_{k}"] for r in rows]))
-                           for k in ("learned", "analytic", "measure")},
+                           for k in ("learned", "analytic", "measure", "cached")},
         "learned_used": int(sum(r["selected_by_learned"] == 1 for r in rows)),
         "exec_time_ratio_learned_over_analytic_geomean":
             g([r["exec_ms_learned"] / r["exec_ms_analytic"] for r in rows]),

@@ -135,7 +135,8 @@ def test_group_separate_member(cuda):
 
 @pytest.mark.parametrize("policy", [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2), (3, 3, 3, 3),
                                     (4, 4, 4, 4), (5, 5, 5, 5), (6, 6, 6, 6), (7, 7, 7, 7),
-                                    (2, 4, 3, 5), (6, 0, 7, 1)])
+                                    (8, 8, 8, 8), (9, 9, 9, 9), (10, 10, 10, 10), (11, 11, 11, 11),
+                                    (2, 4, 3, 5), (6, 0, 7, 1), (10, 8, 4, 2)])
 def test_group_policies(cuda, policy):
     import torch
 
@@ -147,7 +148,7 @@ def test_group_policies(cuda, policy):
     plans = _plans(probs, stream)
     ins, outs = b.ptrs()
     with L.Group(plans, ins, outs, stream, policy=policy) as g:
-        assert g.policy() == (list(policy), False)
+        assert g.policy() == (L.expand_policy(policy), False)
         g.execute()
         b.check()
     for p in plans:
@@ -165,7 +166,7 @@ def test_group_tune_and_cache(cuda):
     with L.Group(plans, ins, outs, stream) as g:
         g.tune()
         pol, tuned = g.policy()
-        assert tuned and all(0 <= x < 8 for x in pol)
+        assert tuned and all(0 <= x < 12 for x in pol)
         b.out.fill_(CANARY)
         g.execute()
         b.check()
@@ -267,5 +268,5 @@ def test_group_errors(cuda):
     assert lib.librett_c_group_tune(987654) == L.LIBRETT_INVALID_PLAN
     with L.Plan([8, 16], [1, 0], 4, s) as p:
         with pytest.raises(L.LibrettError) as e:
-            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 8, 0))
+            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 12, 0))
         assert e.value.code == L.LIBRETT_INVALID_PARAMETER
