@@ -61,9 +61,14 @@ def _compile(src: str, force: bool, verbose: bool, extra: list[str]) -> Path:
 
 
 def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False) -> Path:
-    """Compile every translation unit for sm_103a and link librett.so."""
+    """Compile every translation unit for sm_103a and link librett.so.
+
+    LIBRETT_NVCC_FLAGS (environment) appends flags to every compile, e.g.
+    -DLT_FLAT_ASYNC_MIN_NL=32 to keep every flat tile kernel on register
+    loads; use --force after changing it."""
     BUILD.mkdir(parents=True, exist_ok=True)
     extra = ["-Xptxas", "-v"] if ptxas_verbose else []
+    extra += os.environ.get("LIBRETT_NVCC_FLAGS", "").split()
     workers = min(len(SOURCES), max(1, os.cpu_count() or 1))
     with ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(lambda s: _compile(s, force, verbose, extra), SOURCES))

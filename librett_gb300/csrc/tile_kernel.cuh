@@ -66,6 +66,12 @@ __device__ __forceinline__ void cpAsyncUnit(uint32_t dst, const void* src) {
                  : "memory");
 }
 
+// Flat tile kernels with at least this many load units per thread load
+// through cp.async rather than registers.
+#ifndef LT_FLAT_ASYNC_MIN_NL
+#define LT_FLAT_ASYNC_MIN_NL 8
+#endif
+
 __device__ __forceinline__ void cpAsyncWaitAll() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
@@ -290,16 +296,30 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   T* s = reinterpret_cast<T*>(smraw);
   long long bin, bout;
   decodeTile(p, blockIdx.x, bin, bout);
-  LT v[NL];
+  if constexpr (NL >= LT_FLAT_ASYNC_MIN_NL) {
+    // many load units per thread: cp.async straight into shared memory
+    // instead of NL data registers per thread
+    const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
 #pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    const int u = threadIdx.x + k * TILE_THREADS;
-    if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + __ldg(ldOff + u));
-  }
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < p.nIn)
+        cpAsyncUnit<ES * LV>(sBase + (uint32_t)smemIndex(p, u * LV) * ES,
+                             in + bin + __ldg(ldOff + u));
+    }
+    cpAsyncWaitAll();
+  } else {
+    LT v[NL];
 #pragma unroll
-  for (int k = 0; k < NL; ++k) {
-    const int u = threadIdx.x + k * TILE_THREADS;
-    if (u < p.nIn) *reinterpret_cast<LT*>(s + smemIndex(p, u * LV)) = v[k];
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + __ldg(ldOff + u));
+    }
+#pragma unroll
+    for (int k = 0; k < NL; ++k) {
+      const int u = threadIdx.x + k * TILE_THREADS;
+      if (u < p.nIn) *reinterpret_cast<LT*>(s + smemIndex(p, u * LV)) = v[k];
+    }
   }
   __syncthreads();
   storeTile<ES, SV>(p, stOff, stSm, s, out + bout);
