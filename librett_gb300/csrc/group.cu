@@ -95,6 +95,17 @@ enum GroupPolicy {
   GP_COUNT = 3 * GP_TILES
 };
 constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
+constexpr int STAGE_MAX = 8192;   // largest store-side table set staged in shared memory
+
+// Bytes of a member's store-side run tables (stRow, smRow, smRun) when they
+// are staged in shared memory, else 0.
+int stagedTableBytes(const TileParams& tp) {
+  const GroupRunSplit rs = groupRunSplit(tp);
+  size_t off[4];
+  const size_t total = runTableBytes(tp, rs, off);
+  const size_t bytes = total - off[1];
+  return bytes <= (size_t)STAGE_MAX ? (int)bytes : 0;
+}
 
 // Member class: size class (bytes of one tensor < 64 KiB, < 1 MiB, < 16 MiB,
 // larger) + 4 * element-size index (4, 8, 16 bytes).
@@ -244,6 +255,8 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     out.slots = out.slotsScalar;
     out.smemBytes = out.tile.smStride * out.f.esize;
   }
+  // the tile data plus the staged store-side tables
+  out.smemBytes = out.tile.smStride * out.f.esize + stagedTableBytes(out.tile);
   return out.tile.nGR <= GROUP_MAXG;
 }
 
@@ -367,6 +380,9 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.inRun = makeFastDiv((uint32_t)rs.inRun);
       t.outRun = makeFastDiv((uint32_t)rs.outRun);
       t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
+      t.tabBytes = stagedTableBytes(tp);
+      t.smRowOff = (int)((sub[2] - sub[1]) / 4);
+      t.smRunOff = (int)((sub[3] - sub[1]) / 4);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
       t.nGR = tp.nGR;

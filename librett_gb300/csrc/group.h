@@ -43,6 +43,9 @@ struct GroupTensor {
   int nIn, nOut;       // load / store units of a tile
   FastDiv inRun, outRun;
   FastDiv inSlots;  // aligned 16-byte blocks reserved per input run (loads 2)
+  // Store-side tables staged in shared memory: their bytes (0 = read from
+  // device memory) and the int offsets of smRow and smRun inside them.
+  int tabBytes, smRowOff, smRunOff;
   int padShift, padLog;
   int nGR;
   FastDiv grDiv[GROUP_MAXG];

@@ -330,7 +330,9 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 // decode of its local tile index (same arithmetic as decodeTile).  Unit
 // offsets come from the run split (GroupTensor): a small table entry per
 // run plus the position inside the run, so the tables stay in L1 even when
-// consecutive CTAs belong to different tensors.  LOADS: 0 stages the load
+// consecutive CTAs belong to different tensors; when they are small enough
+// the store-side tables are copied into shared memory with the data.  LOADS:
+// 0 stages the load
 // units in registers; 1 copies them with cp.async straight into shared
 // memory (no data registers, so more CTAs fit an SM); 2, for element-size
 // load units narrower than 16 bytes, reads each input run with aligned
@@ -345,8 +347,10 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ ti
   using LT = typename Word<ES * LV>::T;
   using ST = typename Word<ES * SV>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
-  T* s = reinterpret_cast<T*>(smraw);
   const GroupTensor* g = tens + __ldg(tileTensor + blockIdx.x);
+  // shared memory: [store-side run tables, when staged][tile data]
+  const int tabBytes = g->tabBytes;
+  T* s = reinterpret_cast<T*>(smraw + tabBytes);
   uint32_t rem = blockIdx.x - g->firstTile;
   long long bin = 0, bout = 0;
   const int nGR = g->nGR;
@@ -424,37 +428,51 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ ti
       if (u < nIn) *reinterpret_cast<LT*>(s + pad(u * LV)) = v[k];
     }
   }
+  if (tabBytes > 0) {
+    // the store-side tables (stRow, smRow, smRun are contiguous, 16-byte
+    // aligned) into shared memory, in flight with the data loads
+    const uint32_t tBase = (uint32_t)__cvta_generic_to_shared(smraw);
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(g->stRow);
+    for (int c = threadIdx.x; c < (tabBytes >> 4); c += TILE_THREADS)
+      cpAsyncUnit<16>(tBase + 16u * c, src + 16 * c);
+    cpAsyncWaitAll();
+  }
   __syncthreads();
-  const int* stRow = g->stRow;
-  const int* smRow = g->smRow;
-  const int* smRun = g->smRun;
   const FastDiv outRun = g->outRun;
+  auto storeAll = [&](const int* stRow, const int* smRow, const int* smRun) {
 #pragma unroll 4
-  for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
-    const int q = w * SV;
-    const uint32_t r = fdiv((uint32_t)q, outRun);
-    const int a = q - (int)(r * outRun.d);
-    T* dst = out + a + __ldg(stRow + r);
-    const int jb = __ldg(smRow + r);
-    if constexpr (SV == 1) {
-      *dst = s[pad(jb + __ldg(smRun + a))];
-    } else {
-      T e[SV];
-      if constexpr (SV == 2) {
-        const int2 jr = __ldg(reinterpret_cast<const int2*>(smRun + a));
-        e[0] = s[pad(jb + jr.x)];
-        e[1] = s[pad(jb + jr.y)];
+    for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
+      const int q = w * SV;
+      const uint32_t r = fdiv((uint32_t)q, outRun);
+      const int a = q - (int)(r * outRun.d);
+      T* dst = out + a + stRow[r];
+      const int jb = smRow[r];
+      if constexpr (SV == 1) {
+        *dst = s[pad(jb + smRun[a])];
       } else {
-        const int4 jr = __ldg(reinterpret_cast<const int4*>(smRun + a));
-        e[0] = s[pad(jb + jr.x)];
-        e[1] = s[pad(jb + jr.y)];
-        e[2] = s[pad(jb + jr.z)];
-        e[3] = s[pad(jb + jr.w)];
+        T e[SV];
+        if constexpr (SV == 2) {
+          const int2 jr = *reinterpret_cast<const int2*>(smRun + a);
+          e[0] = s[pad(jb + jr.x)];
+          e[1] = s[pad(jb + jr.y)];
+        } else {
+          const int4 jr = *reinterpret_cast<const int4*>(smRun + a);
+          e[0] = s[pad(jb + jr.x)];
+          e[1] = s[pad(jb + jr.y)];
+          e[2] = s[pad(jb + jr.z)];
+          e[3] = s[pad(jb + jr.w)];
+        }
+        ST val;
+        __builtin_memcpy(&val, e, sizeof(ST));
+        *reinterpret_cast<ST*>(dst) = val;
       }
-      ST val;
-      __builtin_memcpy(&val, e, sizeof(ST));
-      *reinterpret_cast<ST*>(dst) = val;
     }
+  };
+  if (tabBytes > 0) {
+    const int* t = reinterpret_cast<const int*>(smraw);
+    storeAll(t, t + g->smRowOff, t + g->smRunOff);
+  } else {
+    storeAll(g->stRow, g->smRow, g->smRun);
   }
 }
 
