@@ -29,21 +29,23 @@ import librett_gb300 as L
 MIN_LOG2_BYTES, MAX_LOG2_BYTES = 16, 28
 
 
-def problems(n: int, seed: int):
-    """n random problems (dims, perm, element bytes) of the selector's distribution."""
+def problems(n: int, seed: int, min_log2_bytes: float = MIN_LOG2_BYTES,
+             max_log2_bytes: float = MAX_LOG2_BYTES):
+    """n random problems (dims, perm, element bytes) of the selector's distribution
+    (or of the same distribution over another byte range)."""
     rng = np.random.Generator(np.random.MT19937(seed))
     out = []
     while len(out) < n:
         rank = int(rng.integers(2, 8))
         es = int(rng.choice([4, 8, 16]))
-        logbytes = rng.uniform(MIN_LOG2_BYTES, MAX_LOG2_BYTES)
+        logbytes = rng.uniform(min_log2_bytes, max_log2_bytes)
         logvol = logbytes - np.log2(es)
         if logvol < rank:  # every dim >= 2
             continue
         w = rng.uniform(0.05, 1.0, rank)
         logd = w / w.sum() * logvol
         dims = [max(2, int(round(2.0 ** x))) for x in logd]
-        while int(np.prod(dims)) * es > 2 ** MAX_LOG2_BYTES:
+        while int(np.prod(dims)) * es > 2 ** max_log2_bytes:
             i = int(np.argmax(dims))
             dims[i] = max(2, dims[i] // 2)
         perm = [int(x) for x in rng.permutation(rank)]
@@ -118,6 +120,8 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--problems", type=int, default=6000)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--min-log2-bytes", type=float, default=MIN_LOG2_BYTES)
+    ap.add_argument("--max-log2-bytes", type=float, default=MAX_LOG2_BYTES)
     ap.add_argument("--out", required=True)
     args = ap.parse_args(argv)
     import torch
@@ -126,7 +130,7 @@ def main(argv=None):
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     prev = _lib.load().librett_c_set_plan_selector(1)  # heuristic picks = the analytic model
     _lib.load().librett_c_set_candidate_set(1)  # time every pipeline
-    probs = problems(args.problems, args.seed)
+    probs = problems(args.problems, args.seed, args.min_log2_bytes, args.max_log2_bytes)
     data = collect(probs, sms)
     _lib.load().librett_c_set_plan_selector(prev)
     data["sms"] = sms

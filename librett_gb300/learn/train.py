@@ -12,7 +12,7 @@ holds the device buffers and gathers mini-batches.
 
 Usage (on a GPU):
     python -m librett_gb300.learn.train --data data.npz --holdout 1000 \\
-        --out librett_gb300/models/plan_mlp.bin --report report.json
+        [--extra large.npz] --out librett_gb300/models/plan_mlp.bin --report report.json
 """
 from __future__ import annotations
 
@@ -205,6 +205,8 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--out", required=True)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--extra", action="append", default=[],
+                    help="further datasets used for training only (e.g. larger problems)")
     args = ap.parse_args(argv)
     d = np.load(args.data)
     X, t, prob, cand = d["X"], d["t"], d["prob"], d["cand"]
@@ -213,11 +215,18 @@ def main(argv=None):
     split = nprob - args.holdout
     tr, te = prob < split, prob >= split
     y = targets(t, prob)
-    params, mean, std, ymean, ystd, hist = train(X[tr], y[tr], epochs=args.epochs)
+    Xtr, ytr = X[tr], y[tr]
+    extra_problems = 0
+    for path in args.extra:
+        e = np.load(path)
+        Xtr = np.concatenate([Xtr, e["X"]])
+        ytr = np.concatenate([ytr, targets(e["t"], e["prob"])])
+        extra_problems += int(e["prob"].max()) + 1
+    params, mean, std, ymean, ystd, hist = train(Xtr, ytr, epochs=args.epochs)
     save_model(args.out, params, mean, std, ymean, ystd, int(d["sms"]), str(d["device"]))
     pred = predict_gpu(params, (X - mean) / std) * ystd + ymean
-    rep = {"train_problems": int(split), "holdout_problems": int(args.holdout),
-           "rows": int(len(t)), "final_loss": hist[-1]}
+    rep = {"train_problems": int(split), "extra_train_problems": extra_problems,
+           "holdout_problems": int(args.holdout), "rows": int(len(t)), "final_loss": hist[-1]}
     for name, mask in (("train", tr), ("holdout", te)):
         r_mlp = choice_regret(pred[mask], t[mask], prob[mask])
         # analytic model: its pick per problem
