@@ -98,10 +98,9 @@ librettResult librettExecute(librettHandle handle, void* idata, void* odata);
  * ordered on `stream`), writes the tables and instantiates the graph
  * (synchronising `stream` once); execution is one graph launch on `stream`;
  * destruction frees in stream order.  The member plans may be destroyed once
- * the group exists (the group keeps what it needs).  A member runs as a flat
- * tile kernel inside its bucket; one whose pointers are not 16-byte aligned
- * for its vector units, or whose problem needs more than eight grid ranks,
- * runs its own plan's launch inside the same graph instead. */
+ * the group exists (the group keeps what it needs).  Every member runs as a
+ * flat tile inside its bucket (in element units when its pointers are not
+ * 16-byte aligned). */
 typedef unsigned int librettGroupHandle;
 
 librettResult librettGroupCreate(librettGroupHandle* group, int count, const librettHandle* plans,

@@ -68,6 +68,23 @@ __global__ void __launch_bounds__(256) writeGroupTablesKernel(const GroupTableJo
     }
     jb.smRun[a] = jj;
   }
+  // the member's tiles: corner offsets from the grid-rank decode (same
+  // arithmetic as the single-plan kernels' decodeTile), with the descriptor
+  // index in the top bits of the input offset
+  for (uint32_t x = threadIdx.x; x < p.numTiles; x += blockDim.x) {
+    uint32_t rem = x;
+    long long bin = 0, bout = 0;
+    for (int g = 0; g < p.nGR; ++g) {
+      const uint32_t q = fdiv(rem, p.grDiv[g]);
+      const uint32_t c = rem - q * p.grDiv[g].d;
+      rem = q;
+      const bool last = c + 1 == p.grDiv[g].d;
+      bin += last ? p.grLastIn[g] : (long long)c * p.grSin[g];
+      bout += last ? p.grLastOut[g] : (long long)c * p.grSout[g];
+    }
+    jb.tiles[x].inAndTensor = bin | (jb.tensor << GROUP_TILE_SHIFT);
+    jb.tiles[x].out = bout;
+  }
 }
 
 size_t align16(size_t x) { return (x + 15) / 16 * 16; }
@@ -196,7 +213,7 @@ uint64_t fnv(uint64_t h, uint64_t v) {
 }
 
 cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                              const int* map, uint32_t tiles, int smem, cudaStream_t s) {
+                              const GroupTile* map, uint32_t tiles, int smem, cudaStream_t s) {
   switch (es) {
     case 4: return launchGroupTile4(lv, sv, nl, loads, tens, map, tiles, smem, s);
     case 8: return launchGroupTile8(lv, sv, nl, loads, tens, map, tiles, smem, s);
@@ -257,7 +274,7 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
   }
   // the tile data plus the staged store-side tables
   out.smemBytes = out.tile.smStride * out.f.esize + stagedTableBytes(out.tile);
-  return out.tile.nGR <= GROUP_MAXG;
+  return true;
 }
 
 struct Bucket {
@@ -318,9 +335,12 @@ librettResult build(GroupObj& g, const Policy& pol) {
     b.smem = std::max(b.smem, pd.smemBytes);
   }
   B.buckets = (int)buckets.size();
+  // a tile packs its descriptor index above a 40-bit offset
+  for (const Bucket& b : buckets)
+    if (b.members.size() >= (size_t(1) << (63 - GROUP_TILE_SHIFT))) return LIBRETT_INVALID_PARAMETER;
 
-  // one allocation: descriptors, tile maps, table jobs (written from the
-  // host), then the members' offset tables (written by a kernel)
+  // one allocation: descriptors and table jobs (written from the host),
+  // tile lists and the members' run tables (written by a kernel)
   size_t off = 0;
   for (Bucket& b : buckets) {
     b.tensOff = off;
@@ -328,7 +348,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
   }
   for (Bucket& b : buckets) {
     b.mapOff = off;
-    off = align16(off + (size_t)b.tiles * sizeof(int));
+    off = align16(off + (size_t)b.tiles * sizeof(GroupTile));
     B.tiles += b.tiles;
   }
   std::vector<int> jobOf(g.members.size(), -1);
@@ -356,7 +376,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
   GroupTableJob* jobs = reinterpret_cast<GroupTableJob*>(host.data() + jobsOff);
   for (Bucket& b : buckets) {
     GroupTensor* tens = reinterpret_cast<GroupTensor*>(host.data() + b.tensOff);
-    int* map = reinterpret_cast<int*>(host.data() + b.mapOff);
+    GroupTile* map = reinterpret_cast<GroupTile*>(base + b.mapOff);  // device
     uint32_t first = 0;
     for (size_t k = 0; k < b.members.size(); ++k) {
       const int i = b.members[k];
@@ -374,7 +394,6 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.stRow = reinterpret_cast<const int*>(tb + sub[1]);
       t.smRow = reinterpret_cast<const int*>(tb + sub[2]);
       t.smRun = reinterpret_cast<const int*>(tb + sub[3]);
-      t.firstTile = first;
       t.nIn = tp.nIn;
       t.nOut = tp.nOut;
       t.inRun = makeFastDiv((uint32_t)rs.inRun);
@@ -385,16 +404,6 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.smRunOff = (int)((sub[3] - sub[1]) / 4);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
-      t.nGR = tp.nGR;
-      for (int q = 0; q < tp.nGR; ++q) {
-        t.grDiv[q] = tp.grDiv[q];
-        t.grSin[q] = tp.grSin[q];
-        t.grSout[q] = tp.grSout[q];
-        t.grLastIn[q] = tp.grLastIn[q];
-        t.grLastOut[q] = tp.grLastOut[q];
-      }
-      for (uint32_t x = 0; x < tp.numTiles; ++x) map[first + x] = (int)k;
-      first += tp.numTiles;
       GroupTableJob jb;
       std::memset(&jb, 0, sizeof(jb));
       jb.tp = tp;
@@ -403,6 +412,9 @@ librettResult build(GroupObj& g, const Policy& pol) {
       jb.stRow = reinterpret_cast<int*>(tb + sub[1]);
       jb.smRow = reinterpret_cast<int*>(tb + sub[2]);
       jb.smRun = reinterpret_cast<int*>(tb + sub[3]);
+      jb.tiles = map + first;
+      jb.tensor = (long long)k;
+      first += tp.numTiles;
       std::memcpy(jobs + jobOf[i], &jb, sizeof(jb));
     }
   }
@@ -457,7 +469,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
                              (long long)b.tiles, b.bytes});
         launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl, b.loads,
                                      reinterpret_cast<const GroupTensor*>(base + b.tensOff),
-                                     reinterpret_cast<const int*>(base + b.mapOff), b.tiles,
+                                     reinterpret_cast<const GroupTile*>(base + b.mapOff), b.tiles,
                                      b.smem, side[br]) == cudaSuccess;
       } else {
         const Member& m = g.members[-nd.bucket - 1];

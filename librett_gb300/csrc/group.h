@@ -5,9 +5,8 @@
 // Every member runs as a flat tile plan.  Members are bucketed by kernel
 // shape (element size, load unit, store unit, load units per thread); each
 // bucket is one launch over a device-resident descriptor table in which CTA
-// b looks up its tensor (tileTensor[b]) and that tensor's descriptor
-// (pointers, offset tables, grid-rank decode).  Members that do not fit the
-// compact descriptor run with their own launch inside the same graph.
+// b reads its tile (tensor index and corner offsets) and that tensor's
+// descriptor (pointers, run tables).
 //
 // Which flat tile a member gets, and whether its bucket loads through
 // registers or cp.async, is a policy per member class (size and element
@@ -26,7 +25,6 @@
 
 namespace lt {
 
-constexpr int GROUP_MAXG = 8;     // grid ranks a compact descriptor holds
 // Member classes of the tile-policy autotuner: 4 size classes (bytes of one
 // tensor < 64 KiB, < 1 MiB, < 16 MiB, larger) x 3 element sizes (4, 8, 16);
 // class = size class + 4 * log2(element bytes / 4).
@@ -39,7 +37,6 @@ struct GroupTensor {
   const int* stRow;  // [tileVol / outRun] output offset of each output run
   const int* smRow;  // [tileVol / outRun] in-tile index of each output run's first element
   const int* smRun;  // [outRun] in-tile index of each element of an output run, from the first
-  uint32_t firstTile;  // index of this tensor's first tile in the bucket
   int nIn, nOut;       // load / store units of a tile
   FastDiv inRun, outRun;
   FastDiv inSlots;  // aligned 16-byte blocks reserved per input run (loads 2)
@@ -47,11 +44,18 @@ struct GroupTensor {
   // device memory) and the int offsets of smRow and smRun inside them.
   int tabBytes, smRowOff, smRunOff;
   int padShift, padLog;
-  int nGR;
-  FastDiv grDiv[GROUP_MAXG];
-  long long grSin[GROUP_MAXG], grSout[GROUP_MAXG];
-  long long grLastIn[GROUP_MAXG], grLastOut[GROUP_MAXG];
 };
+
+// One tile of a bucket, written on the device at group creation: the
+// element offset of its input corner with its tensor's descriptor index in
+// the top 24 bits (offsets are < 2^40 elements), and the element offset of
+// its output corner.  A CTA reads its tile with one 16-byte load instead of
+// decoding the grid ranks.
+struct GroupTile {
+  long long inAndTensor;
+  long long out;
+};
+constexpr int GROUP_TILE_SHIFT = 40;
 
 // Run-table job for one member (written once, at group creation).
 struct GroupTableJob {
@@ -61,16 +65,18 @@ struct GroupTableJob {
   int* stRow;
   int* smRow;
   int* smRun;
+  GroupTile* tiles;  // this member's tiles in its bucket's tile list
+  long long tensor;  // descriptor index in the bucket
 };
 
 // Launch of one bucket's kernel (defined per element size in k_tile*.cu);
 // loads: 0 registers, 1 cp.async, 2 aligned 16-byte run reads (element-size
 // load units narrower than 16 bytes only).
 cudaError_t launchGroupTile4(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                             const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
+                             const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
 cudaError_t launchGroupTile8(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                             const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
+                             const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
 cudaError_t launchGroupTile16(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                              const int* tileTensor, uint32_t numTiles, int smem, cudaStream_t s);
+                              const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
 
 }  // namespace lt

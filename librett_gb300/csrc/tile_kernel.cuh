@@ -326,8 +326,8 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 }
 
 // Grouped flat kernel: CTA b moves one tile of tensor tileTensor[b] of a
-// bucket; the tensor's descriptor gives its pointers, run tables and the
-// decode of its local tile index (same arithmetic as decodeTile).  Unit
+// bucket; the tile list gives the tensor and the tile's corner offsets, the
+// tensor's descriptor its pointers and run tables.  Unit
 // offsets come from the run split (GroupTensor): a small table entry per
 // run plus the position inside the run, so the tables stay in L1 even when
 // consecutive CTAs belong to different tensors; when they are small enough
@@ -342,31 +342,17 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 // the block extends past the tensor; the bytes outside the run are dropped.
 template <int ES, int LV, int SV, int NL, int LOADS>
 __global__ void __launch_bounds__(TILE_THREADS)
-groupTileKernel(const GroupTensor* __restrict__ tens, const int* __restrict__ tileTensor) {
+groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restrict__ tiles) {
   using T = typename Word<ES>::T;
   using LT = typename Word<ES * LV>::T;
   using ST = typename Word<ES * SV>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const GroupTensor* g = tens + __ldg(tileTensor + blockIdx.x);
+  const longlong2 tile = __ldg(reinterpret_cast<const longlong2*>(tiles) + blockIdx.x);
+  const GroupTensor* g = tens + (int)(tile.x >> GROUP_TILE_SHIFT);
+  const long long bin = tile.x & ((1LL << GROUP_TILE_SHIFT) - 1), bout = tile.y;
   // shared memory: [store-side run tables, when staged][tile data]
   const int tabBytes = g->tabBytes;
   T* s = reinterpret_cast<T*>(smraw + tabBytes);
-  uint32_t rem = blockIdx.x - g->firstTile;
-  long long bin = 0, bout = 0;
-  const int nGR = g->nGR;
-  // unrolled with a predicate so that the descriptor loads issue together
-#pragma unroll
-  for (int k = 0; k < GROUP_MAXG; ++k) {
-    if (k < nGR) {
-      const FastDiv dv = g->grDiv[k];
-      const uint32_t q = fdiv(rem, dv);
-      const uint32_t c = rem - q * dv.d;
-      rem = q;
-      const bool last = c + 1 == dv.d;
-      bin += last ? g->grLastIn[k] : (long long)c * g->grSin[k];
-      bout += last ? g->grLastOut[k] : (long long)c * g->grSout[k];
-    }
-  }
   const T* in = reinterpret_cast<const T*>(g->in) + bin;
   T* out = reinterpret_cast<T*>(g->out) + bout;
   const int* ldRow = g->ldRow;

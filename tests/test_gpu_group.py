@@ -5,8 +5,7 @@ its own offset with a canary-filled gap behind it.  After the group runs,
 every tensor must equal the oracle's transpose bit for bit and every gap must
 still hold the canary.  Covered: mixed ranks, permutations and element sizes
 (4/8/16 bytes); members whose pointers are not 16-byte aligned (element
-units inside their bucket); a member needing more grid ranks than the
-compact descriptor holds (its plan's own launch inside the graph); a second
+units inside their bucket); a rank-16 member with many grid ranks; a second
 execution after the inputs changed (the graph reads the buffers anew); plans
 destroyed before the group runs; every tile policy and the autotuner; the
 one-shot librettExecuteGrouped; the plain per-tensor loop; and the error
@@ -116,17 +115,18 @@ def test_group_mixed_bit_exact(cuda):
     assert L.launch_count() > before
 
 
-def test_group_separate_member(cuda):
+def test_group_high_rank_member(cuda):
     import torch
 
-    # 16 unfusable ranks: every flat tile leaves more than eight grid ranks
+    # 16 unfusable ranks: every flat tile leaves nine or more grid ranks,
+    # whose decode the group does once per tile at creation
     probs = [([3] * 16, list(range(15, -1, -1)), 4)] + _mixed_problems(20, seed=21)
     b = _Batch(probs, [False] * len(probs), seed=9)
     stream = torch.cuda.current_stream()
     plans = _plans(probs, stream)
     ins, outs = b.ptrs()
     with L.Group(plans, ins, outs, stream) as g:
-        assert g.info()["separate"] == 1
+        assert g.info()["separate"] == 0
         g.execute()
         b.check()
     for p in plans:
