@@ -54,8 +54,7 @@ __global__ void __launch_bounds__(256) writeGroupTablesKernel(const GroupTableJo
       off += c * p.trSout[t];
       jj += c * p.trInTile[t];
     }
-    jb.stRow[r] = off;
-    jb.smRow[r] = jj;
+    jb.outRows[r] = make_int2(off, jj);
   }
   for (int a = threadIdx.x; a < rs.outRun; a += blockDim.x) {
     int rem = a, jj = 0;
@@ -89,14 +88,14 @@ __global__ void __launch_bounds__(256) writeGroupTablesKernel(const GroupTableJo
 
 size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 
-// Bytes of a member's run tables; sub-table offsets (16-byte aligned).
-size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[4]) {
+// Bytes of a member's run tables; sub-table offsets (16-byte aligned):
+// ldRow at off[0], outRows at off[1], smRun at off[2].
+size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[3]) {
   const size_t nL = tp.tileVol / rs.inRun, nS = tp.tileVol / rs.outRun;
   off[0] = 0;
   off[1] = align16(4 * nL);
-  off[2] = off[1] + align16(4 * nS);
-  off[3] = off[2] + align16(4 * nS);
-  return off[3] + align16(4 * (size_t)rs.outRun);
+  off[2] = off[1] + align16(8 * nS);
+  return off[2] + align16(4 * (size_t)rs.outRun);
 }
 
 // Policies: policy % GP_TILES picks a member's flat tile from its
@@ -114,11 +113,11 @@ enum GroupPolicy {
 constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
 constexpr int STAGE_MAX = 8192;   // largest store-side table set staged in shared memory
 
-// Bytes of a member's store-side run tables (stRow, smRow, smRun) when they
-// are staged in shared memory, else 0.
+// Bytes of a member's store-side run tables (outRows, smRun) when they are
+// staged in shared memory, else 0.
 int stagedTableBytes(const TileParams& tp) {
   const GroupRunSplit rs = groupRunSplit(tp);
-  size_t off[4];
+  size_t off[3];
   const size_t total = runTableBytes(tp, rs, off);
   const size_t bytes = total - off[1];
   return bytes <= (size_t)STAGE_MAX ? (int)bytes : 0;
@@ -361,7 +360,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
   std::vector<size_t> tabOff(g.members.size(), 0);
   for (const Bucket& b : buckets)
     for (int i : b.members) {
-      size_t sub[4];
+      size_t sub[3];
       const TileParams& tp = g.members[i].pd.tile;
       tabOff[i] = off;
       off = align16(off + runTableBytes(tp, groupRunSplit(tp), sub));
@@ -383,7 +382,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       const Member& m = g.members[i];
       const TileParams& tp = m.pd.tile;
       const GroupRunSplit rs = groupRunSplit(tp);
-      size_t sub[4];
+      size_t sub[3];
       runTableBytes(tp, rs, sub);
       unsigned char* tb = base + tabOff[i];
       GroupTensor& t = tens[k];
@@ -391,17 +390,15 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.in = m.in;
       t.out = m.out;
       t.ldRow = reinterpret_cast<const int*>(tb + sub[0]);
-      t.stRow = reinterpret_cast<const int*>(tb + sub[1]);
-      t.smRow = reinterpret_cast<const int*>(tb + sub[2]);
-      t.smRun = reinterpret_cast<const int*>(tb + sub[3]);
+      t.outRows = reinterpret_cast<const int2*>(tb + sub[1]);
+      t.smRun = reinterpret_cast<const int*>(tb + sub[2]);
       t.nIn = tp.nIn;
       t.nOut = tp.nOut;
       t.inRun = makeFastDiv((uint32_t)rs.inRun);
       t.outRun = makeFastDiv((uint32_t)rs.outRun);
       t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
       t.tabBytes = stagedTableBytes(tp);
-      t.smRowOff = (int)((sub[2] - sub[1]) / 4);
-      t.smRunOff = (int)((sub[3] - sub[1]) / 4);
+      t.smRunOff = (int)((sub[2] - sub[1]) / 4);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
       GroupTableJob jb;
@@ -409,9 +406,8 @@ librettResult build(GroupObj& g, const Policy& pol) {
       jb.tp = tp;
       jb.rs = rs;
       jb.ldRow = reinterpret_cast<int*>(tb + sub[0]);
-      jb.stRow = reinterpret_cast<int*>(tb + sub[1]);
-      jb.smRow = reinterpret_cast<int*>(tb + sub[2]);
-      jb.smRun = reinterpret_cast<int*>(tb + sub[3]);
+      jb.outRows = reinterpret_cast<int2*>(tb + sub[1]);
+      jb.smRun = reinterpret_cast<int*>(tb + sub[2]);
       jb.tiles = map + first;
       jb.tensor = (long long)k;
       first += tp.numTiles;

@@ -34,15 +34,16 @@ struct GroupTensor {
   const unsigned char* in;
   unsigned char* out;
   const int* ldRow;  // [tileVol / inRun]  input offset of each input run
-  const int* stRow;  // [tileVol / outRun] output offset of each output run
-  const int* smRow;  // [tileVol / outRun] in-tile index of each output run's first element
+  // [tileVol / outRun] per output run: output offset, in-tile index of its
+  // first element
+  const int2* outRows;
   const int* smRun;  // [outRun] in-tile index of each element of an output run, from the first
   int nIn, nOut;       // load / store units of a tile
   FastDiv inRun, outRun;
   FastDiv inSlots;  // aligned 16-byte blocks reserved per input run (loads 2)
   // Store-side tables staged in shared memory: their bytes (0 = read from
-  // device memory) and the int offsets of smRow and smRun inside them.
-  int tabBytes, smRowOff, smRunOff;
+  // device memory) and the int offset of smRun inside them (outRows first).
+  int tabBytes, smRunOff;
   int padShift, padLog;
 };
 
@@ -62,8 +63,7 @@ struct GroupTableJob {
   TileParams tp;
   GroupRunSplit rs;
   int* ldRow;
-  int* stRow;
-  int* smRow;
+  int2* outRows;
   int* smRun;
   GroupTile* tiles;  // this member's tiles in its bucket's tile list
   long long tensor;  // descriptor index in the bucket

@@ -415,24 +415,25 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
     }
   }
   if (tabBytes > 0) {
-    // the store-side tables (stRow, smRow, smRun are contiguous, 16-byte
+    // the store-side tables (outRows and smRun are contiguous, 16-byte
     // aligned) into shared memory, in flight with the data loads
     const uint32_t tBase = (uint32_t)__cvta_generic_to_shared(smraw);
-    const unsigned char* src = reinterpret_cast<const unsigned char*>(g->stRow);
+    const unsigned char* src = reinterpret_cast<const unsigned char*>(g->outRows);
     for (int c = threadIdx.x; c < (tabBytes >> 4); c += TILE_THREADS)
       cpAsyncUnit<16>(tBase + 16u * c, src + 16 * c);
     cpAsyncWaitAll();
   }
   __syncthreads();
   const FastDiv outRun = g->outRun;
-  auto storeAll = [&](const int* stRow, const int* smRow, const int* smRun) {
+  auto storeAll = [&](const int2* outRows, const int* smRun) {
 #pragma unroll 4
     for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
       const int q = w * SV;
       const uint32_t r = fdiv((uint32_t)q, outRun);
       const int a = q - (int)(r * outRun.d);
-      T* dst = out + a + stRow[r];
-      const int jb = smRow[r];
+      const int2 row = outRows[r];
+      T* dst = out + a + row.x;
+      const int jb = row.y;
       if constexpr (SV == 1) {
         *dst = s[pad(jb + smRun[a])];
       } else {
@@ -456,9 +457,9 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
   };
   if (tabBytes > 0) {
     const int* t = reinterpret_cast<const int*>(smraw);
-    storeAll(t, t + g->smRowOff, t + g->smRunOff);
+    storeAll(reinterpret_cast<const int2*>(smraw), t + g->smRunOff);
   } else {
-    storeAll(g->stRow, g->smRow, g->smRun);
+    storeAll(g->outRows, g->smRun);
   }
 }
 
