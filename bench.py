@@ -309,6 +309,35 @@ def traffic_from_profiles(workload):
         return None
 
 
+def copy_ceiling(inp, out, stream, nbytes, reps=10):
+    """Copy ceilings measured in the same run (the role of LibreTT's
+    bench memcpy mode, tests/librett_bench.cpp:879-955): cudaMemcpyAsync
+    device to device, and this engine's own copy kernel (a rank-1 plan), each
+    the best of `reps` event-timed copies of nbytes; GB/s = 2 * bytes / t."""
+    import torch
+
+    import librett_gb300 as L
+
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def best(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            ev[0].record(stream)
+            fn()
+            ev[1].record(stream)
+            ev[1].synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        return 2 * nbytes / (min(ts) / 1e3) / 1e9
+
+    memcpy = best(lambda: out[:nbytes].copy_(inp[:nbytes], non_blocking=True))
+    with L.Plan([nbytes // 8], [0], 8, stream) as p:
+        engine = best(lambda: p.execute(inp.data_ptr(), out.data_ptr()))
+    return {"cuda_memcpy_d2d_gbs": round(memcpy, 1), "engine_copy_kernel_gbs": round(engine, 1),
+            "bytes": nbytes, "how": f"best of {reps}, 2*bytes/time"}
+
+
 def run_engine(args):
     import torch
 
@@ -392,6 +421,7 @@ def run_engine(args):
         traffic = prof.get("dram_bytes_per_launch")
     geo = float(np.exp(np.mean([np.log(2 * problem_bytes(p) / (t / 1e3) / 1e9)
                                 for p, t in zip(problems, per_problem_ms)])))
+    ceiling = copy_ceiling(inp, out, stream, (maxb // 8) * 8) if maxb >= 1 << 26 else None
 
     # end to end through the public API: pinned host in -> device -> host out
     e2e = None
@@ -458,7 +488,8 @@ def run_engine(args):
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind,
                      "traffic": traffic,
-                     "algorithmic_bytes_per_launch": d["bytes"] // d["launches"]},
+                     "algorithmic_bytes_per_launch": d["bytes"] // d["launches"],
+                     "copy_ceiling_same_run": ceiling},
         "per_kernel": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                            "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)}
                        for k, v in per_kernel.items()},
