@@ -84,8 +84,15 @@ cudaError_t launchRowsUnit(int unit, const RowParams& rp, const void* in, void* 
 
 }  // namespace
 
+// The tile fields the table writer needs (about a third of TileParams, so
+// the launch carries a small parameter block).
+struct TableParams {
+  int tileVol, lv, sv, nIn, nTR, padShift, padLog;
+  int trE[MAXR], trInTile[MAXR], trSin[MAXR], trSout[MAXR], trOut[MAXR];
+};
+
 __global__ void __launch_bounds__(256)
-writeTileTablesKernel(const __grid_constant__ TileParams p, int* ldOff, int* stOff,
+writeTileTablesKernel(const __grid_constant__ TableParams p, int* ldOff, int* stOff,
                       unsigned short* stSm) {
   const int stride = gridDim.x * blockDim.x;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < p.nIn; u += stride) {
@@ -129,12 +136,64 @@ cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStr
   int* ld = reinterpret_cast<int*>(base);
   int* st = reinterpret_cast<int*>(base + stOffset);
   unsigned short* sm = reinterpret_cast<unsigned short*>(base + smOffset);
-  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(tp, ld, st, sm);
+  TableParams p;
+  p.tileVol = tp.tileVol;
+  p.lv = tp.lv;
+  p.sv = tp.sv;
+  p.nIn = tp.nIn;
+  p.nTR = tp.nTR;
+  p.padShift = tp.padShift;
+  p.padLog = tp.padLog;
+  for (int t = 0; t < MAXR; ++t) {
+    p.trE[t] = tp.trE[t];
+    p.trInTile[t] = tp.trInTile[t];
+    p.trSin[t] = tp.trSin[t];
+    p.trSout[t] = tp.trSout[t];
+    p.trOut[t] = tp.trOut[t];
+  }
+  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(p, ld, st, sm);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   dt->ldOff = ld;
   dt->stOff = st;
   dt->stSm = sm;
+  return cudaSuccess;
+}
+
+// Plan tables come from a memory pool of the library's own per device, which
+// keeps up to TABLE_POOL_KEEP bytes of freed blocks for reuse instead of
+// returning them to the device at every synchronisation (what the default
+// pool does), so creating a plan does not map fresh memory each time.  The
+// pools live until the process exits.
+constexpr uint64_t TABLE_POOL_KEEP = 256ull << 20;
+
+cudaError_t tablePool(cudaMemPool_t* pool) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) {
+    *pool = it->second;
+    return cudaSuccess;
+  }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t p = nullptr;
+  err = cudaMemPoolCreate(&p, &props);
+  if (err != cudaSuccess) return err;
+  uint64_t keep = TABLE_POOL_KEEP;
+  err = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (err != cudaSuccess) {
+    cudaMemPoolDestroy(p);
+    return err;
+  }
+  pools[dev] = p;
+  *pool = p;
   return cudaSuccess;
 }
 
@@ -145,7 +204,10 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
   size_t stOffset, smOffset;
   const size_t total = deviceTableBytes(pd.tile, &stOffset, &smOffset);
   void* d = nullptr;
-  cudaError_t err = cudaMallocAsync(&d, total, s);
+  cudaMemPool_t pool = nullptr;
+  cudaError_t err = tablePool(&pool);
+  if (err != cudaSuccess) return err;
+  err = cudaMallocFromPoolAsync(&d, total, pool, s);
   if (err != cudaSuccess) return err;
   // the tables are computed on the device, in stream order before any use
   err = writeDeviceTables(pd.tile, static_cast<unsigned char*>(d), s, dt);

@@ -15,8 +15,8 @@ struct DeviceTables {
   const unsigned short* stSm = nullptr;
 };
 
-// Builds the plan's tables on the host and uploads them into one
-// stream-ordered device allocation (cudaMallocAsync on s).  Plans of other
+// Allocates the plan's tables stream-ordered on s (from the library's
+// per-device table pool) and writes them with a kernel on s.  Plans of other
 // pipelines need none: *alloc = nullptr.
 cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt);
 
