@@ -218,11 +218,13 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
       ++gCacheMisses;
     }
   }
-  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  // rank the screened candidates, then complete the chosen one
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms, true);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   bool learned = false;
   int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName.c_str(), &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  if (!lt::refineCandidate(cands[pick], sms)) return LIBRETT_INTERNAL_ERROR;
   const int selectedBy = candidate >= 0 ? 3 : (learned ? 1 : 0);
   if (candidate < 0) {
     std::lock_guard<std::mutex> lk(gCacheMu);
@@ -397,11 +399,12 @@ int librett_c_describe(int rank, const int* dim, const int* permutation, size_t 
   lt::Fused f;
   lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
   const int sms = num_sms > 0 ? num_sms : 152;
-  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms, true);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   bool learned = false;
   int pick = candidate < 0 ? lt::choosePlan(cands, sms, nullptr, &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  if (!lt::refineCandidate(cands[pick], sms)) return LIBRETT_INTERNAL_ERROR;
   fillInfo(cands[pick], 0, info);
   info->selected_by = candidate >= 0 ? 3 : (learned ? 1 : 0);
   return LIBRETT_SUCCESS;
@@ -460,7 +463,8 @@ int librett_c_candidate_features(int rank, const int* dim, const int* permutatio
   lt::Fused f;
   lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
   const int sms = num_sms > 0 ? num_sms : 152;
-  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms);
+  // the features the selectors see: of the screened candidate
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms, true);
   if (candidate < 0 || candidate >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
   lt::planFeatures(cands[candidate], sms, features);
   return LIBRETT_SUCCESS;

@@ -229,7 +229,9 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
   if (policy == GP_SELECTOR && own.kernel == K_TILE && own.pipe == PIPE_FLAT) {
     out = own;
   } else {
-    std::vector<PlanDesc> c = flatTileCandidates(own.f, policy == GP_FILL ? sms * 64 : sms);
+    // the selector ranks screened candidates (as for librettPlan)
+    std::vector<PlanDesc> c =
+        flatTileCandidates(own.f, policy == GP_FILL ? sms * 64 : sms, policy == GP_SELECTOR);
     if (c.empty()) return false;
     int k = 0;
     auto eff = [](const PlanDesc& p) { return std::min(p.effIn, p.effOut); };
@@ -260,6 +262,7 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
         break;
     }
     out = c[k];
+    if (!refineCandidate(out, sms)) return false;
   }
   const GroupRunSplit rs = groupRunSplit(out.tile);
   const bool unitsFit = rs.inRun % out.tile.lv == 0 && rs.outRun % out.tile.sv == 0;

@@ -87,7 +87,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
 
   Fused f;
   fuseRanks(rank, dim, permutation, (int)sizeofType, f);
-  std::vector<PlanDesc> cands = enumerateCandidates(f, ds.numSMs);
+  std::vector<PlanDesc> cands = enumerateCandidates(f, ds.numSMs, true);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   int pick = choosePlan(cands, ds.numSMs, nullptr, nullptr);
   // Tile problems run the flat pipeline, whose tables go to the scratch.
@@ -99,7 +99,8 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
         flat = (int)c;
     if (flat >= 0) pick = flat;
   }
-  if (!finalizePlan(cands[pick])) return LIBRETT_INTERNAL_ERROR;
+  if (!refineCandidate(cands[pick], ds.numSMs) || !finalizePlan(cands[pick]))
+    return LIBRETT_INTERNAL_ERROR;
   const PlanDesc& pd = cands[pick];
   DeviceTables dt;
   const bool vecOk = ((uintptr_t)idata % 16 == 0 && (uintptr_t)odata % 16 == 0) ||

@@ -420,7 +420,8 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide) {
 // and the padding that minimises shared-memory bank wavefronts.  Shared by
 // the three pipelines.  Returns false when the tile does not fit the
 // kernels' limits.
-bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp) {
+bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp,
+                       bool padSearch = true) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
@@ -483,11 +484,20 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   const int sIn = std::min(tp.nIn, 64), sOut = std::min(tp.nOut, 64);
   const long long bound = ((sIn + 31) / 32) * std::max(1, words * lv) +
                           ((sOut + 31) / 32) * sv * std::max(1, words);
+  if (!padSearch) {
+    // Screening skips the padding search unless some padding could push
+    // the tile past the shared-index or shared-memory limits; then the
+    // search decides feasibility exactly as a full enumeration would.
+    const int worst = tp.tileVol + ((tp.tileVol >> 2) << tp.padLog) + 16;
+    const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
+    if (worst > 65535 || tableBytes + TILE_STAGES * worst * f.esize > 227 * 1024) padSearch = true;
+  }
+  tp.screened = padSearch ? 0 : 1;
   int nStore = 0;
   const std::vector<int> jStore = storeSample(tp, 64, nStore);
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
-    if (sh < tp.padLog) continue;
+    if (sh < tp.padLog || (!padSearch && sh != PAD_NONE)) continue;
     long long w = wavefronts(tp, f.esize, sh, 64, jStore, nStore);
     if (best < 0 || w < best) {
       best = w;
@@ -725,7 +735,8 @@ void modelRows(PlanDesc& pd, int numSMs) {
 // Tile candidates: (target contiguous run bytes, maximum tile bytes,
 // minimum tile bytes), each in the flat pipeline and, unless flatOnly, the
 // two persistent pipelines.
-void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out) {
+void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out,
+                          bool screen) {
   const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
                           {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
                           {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
@@ -741,13 +752,14 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
     if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
     seen.push_back(key);
     TileParams geom;
-    if (!buildTileGeometry(f, e, V, V, geom)) continue;
+    if (!buildTileGeometry(f, e, V, V, geom, !screen)) continue;
     for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
       if (pipe != PIPE_FLAT && flatOnly) continue;
       PlanDesc pd;
       pd.f = f;
       pd.targetRunBytes = kb[0];
       pd.maxTileBytes = kb[1];
+      pd.screened = geom.screened != 0;
       if (!buildTile(f, e, pipe, geom, pd)) continue;
       modelTile(pd, numSMs);
       out.push_back(pd);
@@ -755,10 +767,10 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
   }
 }
 
-std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs) {
+std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs, bool screen) {
   std::vector<PlanDesc> out;
   out.reserve(12);
-  appendTileCandidates(f, numSMs < 1 ? 1 : numSMs, true, out);
+  appendTileCandidates(f, numSMs < 1 ? 1 : numSMs, true, out, screen);
   for (size_t i = 0; i < out.size(); ++i) {
     out[i].candidate = (int)i;
     out[i].numCandidates = (int)out.size();
@@ -782,7 +794,7 @@ bool allPipelines() {
   return v == 1;
 }
 
-std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
+std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool screen) {
   std::vector<PlanDesc> out;
   out.reserve(allPipelines() ? 32 : 12);
   if (numSMs < 1) numSMs = 1;
@@ -818,13 +830,30 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs) {
         out.push_back(pd);
       }
     }
-    appendTileCandidates(f, numSMs, !allPipelines(), out);
+    appendTileCandidates(f, numSMs, !allPipelines(), out, screen);
   }
   for (size_t i = 0; i < out.size(); ++i) {
     out[i].candidate = (int)i;
     out[i].numCandidates = (int)out.size();
   }
   return out;
+}
+
+bool refineCandidate(PlanDesc& pd, int numSMs) {
+  if (pd.kernel != K_TILE || !pd.screened) return true;
+  const int V = 16 / pd.f.esize;
+  TileParams geom;
+  if (!buildTileGeometry(pd.f, pd.extent, V, V, geom, true)) return false;
+  PlanDesc full;
+  full.f = pd.f;
+  full.targetRunBytes = pd.targetRunBytes;
+  full.maxTileBytes = pd.maxTileBytes;
+  if (!buildTile(pd.f, pd.extent, pd.pipe, geom, full)) return false;
+  modelTile(full, numSMs < 1 ? 1 : numSMs);
+  full.candidate = pd.candidate;
+  full.numCandidates = pd.numCandidates;
+  pd = full;
+  return true;
 }
 
 bool finalizePlan(PlanDesc& pd) {

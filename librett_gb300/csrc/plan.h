@@ -89,6 +89,7 @@ struct TileParams {
   int smStride;         // elements per smem buffer including padding
   int nRagged;          // grid ranks whose dim is not a multiple of the extent
   int bankWavefronts;   // planner only: simulated wavefronts at padShift
+  int screened;         // planner only: built without the padding search
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
@@ -140,6 +141,7 @@ struct PlanDesc {
   int candidate = 0;
   int numCandidates = 0;
   int targetRunBytes = 0, maxTileBytes = 0;  // knobs that produced the tile
+  bool screened = false;   // tile built without the padding search (refineCandidate)
   // model statistics (also features of the learned selector)
   double effIn = 1.0, effOut = 1.0;  // useful bytes / DRAM sector bytes per side
   double overlap = 1.0;              // elements moved / volume (shifted chunks)
@@ -167,15 +169,22 @@ void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
 // default tile candidates use the flat pipeline only (it wins on nearly all
 // measured problems); setAllPipelines(true) or LIBRETT_ALL_PIPELINES=1 adds
 // the persistent register-staged and cp.async variants.
-std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs);
+//
+// screen: build tile candidates without the shared-memory padding search
+// (padding off, bank wavefronts of the unpadded tile), the form the plan
+// selectors rank; refineCandidate() then completes the chosen one, giving
+// exactly the candidate a full enumeration would have built.
+std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool screen = false);
+bool refineCandidate(PlanDesc& pd, int numSMs);
 void setAllPipelines(bool all);
 bool allPipelines();
 
 // Tile candidates in the one-tile-per-CTA pipeline only, for any fused
 // problem (a fused rank-1 copy becomes a one-rank tile); used where every
 // member of a batch must run in that pipeline (grouped execution).
-std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs);
-void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out);
+std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs, bool screen = false);
+void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out,
+                          bool screen = false);
 
 // Index of the candidate the analytic model prefers.
 int chooseHeuristic(const std::vector<PlanDesc>& cands);

@@ -12,6 +12,12 @@ time is the median batch time / R.
 
 Usage (on a GPU):
     python -m librett_gb300.learn.data --problems 6000 --seed 7 --out data.npz
+Recomputing the features of a collected dataset (host only):
+    python -m librett_gb300.learn.data --refeature data.npz --out data2.npz
+Both datasets from the committed timings (host only; writes data.npz and
+data_large.npz):
+    python -m librett_gb300.learn.data \
+        --from-timings librett_gb300/models/plan_timings_gb300.npz --out data.npz
 """
 from __future__ import annotations
 
@@ -116,6 +122,40 @@ def collect(probs, num_sms, log_every=200):
             "problems": json.dumps(probs)}
 
 
+def refeature(d):
+    """Recompute the features and the analytic model's picks of a dataset
+    from its problems and candidate indices with the current library (the
+    timings stay; candidates are numbered as with every pipeline on)."""
+    lib = _lib.load()
+    probs = [tuple(x) for x in json.loads(str(d["problems"]))]
+    sms = int(d["sms"])
+    prev_sel = lib.librett_c_set_plan_selector(1)
+    prev_set = lib.librett_c_set_candidate_set(1)
+    try:
+        X = np.stack([features(*probs[int(p)], int(c), sms) for p, c in zip(d["prob"], d["cand"])])
+        heur = np.array([L.describe(dims, perm, es, num_sms=sms)["candidate"]
+                         for dims, perm, es in probs])
+    finally:
+        lib.librett_c_set_candidate_set(prev_set)
+        lib.librett_c_set_plan_selector(prev_sel)
+    out = {k: d[k] for k in d}
+    out["X"] = X.astype(np.float32)
+    out["heuristic"] = heur
+    return out
+
+
+def from_timings(path):
+    """The two datasets (base distribution, large-problem supplement) of a
+    committed timing file (librett_gb300/models/plan_timings_*.npz), with
+    features computed by the current library."""
+    z = np.load(path)
+    base = {"problems": z["problems"], "prob": z["prob"], "cand": z["cand"], "t": z["t"],
+            "sms": z["sms"], "device": z["device"]}
+    large = {"problems": z["large_problems"], "prob": z["large_prob"], "cand": z["large_cand"],
+             "t": z["large_t"], "sms": z["sms"], "device": z["device"]}
+    return refeature(base), refeature(large)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--problems", type=int, default=6000)
@@ -123,7 +163,25 @@ def main(argv=None):
     ap.add_argument("--min-log2-bytes", type=float, default=MIN_LOG2_BYTES)
     ap.add_argument("--max-log2-bytes", type=float, default=MAX_LOG2_BYTES)
     ap.add_argument("--out", required=True)
+    ap.add_argument("--refeature", default=None,
+                    help="recompute features of this dataset (no GPU needed) instead of timing")
+    ap.add_argument("--from-timings", default=None,
+                    help="build both datasets from a committed timing file (no GPU needed)")
     args = ap.parse_args(argv)
+    if args.refeature:
+        z = np.load(args.refeature)
+        data = refeature({k: z[k] for k in z.files})
+        np.savez_compressed(args.out, **data)
+        print(f"wrote {args.out}: {len(data['t'])} rows")
+        return 0
+    if args.from_timings:
+        base, large = from_timings(args.from_timings)
+        stem = args.out[:-4] if args.out.endswith(".npz") else args.out
+        np.savez_compressed(args.out, **base)
+        np.savez_compressed(stem + "_large.npz", **large)
+        print(f"wrote {args.out} ({len(base['t'])} rows) and {stem}_large.npz "
+              f"({len(large['t'])} rows)")
+        return 0
     import torch
 
     torch.cuda.set_device(0)
