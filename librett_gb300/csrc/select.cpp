@@ -190,37 +190,33 @@ inline F4 load4(const float* p) {
 }
 
 // y[r] = relu(b + x[r] . wt) for n rows, wt stored input-major (wt[i][o]).
-// Register-blocked: two rows by 16 outputs accumulate in registers over the
-// inputs; each output's sum runs in input order starting from the bias.
+// Register-blocked: four rows by 16 outputs accumulate in registers over the
+// inputs (each weight vector loaded once per four rows); each output's sum
+// runs in input order starting from the bias.
 void denseRelu(const float* x, int n, int in, const float* wt, const float* b, float* y) {
-  constexpr int OB = 16, NV = OB / 4;
+  constexpr int RB = 4, OB = 16, NV = OB / 4;
   const F4 zero = {0.f, 0.f, 0.f, 0.f};
-  for (int r0 = 0; r0 < n; r0 += 2) {
-    const bool two = r0 + 1 < n;
-    const float* x0 = x + (size_t)r0 * in;
-    const float* x1 = two ? x0 + in : x0;
-    float* y0 = y + (size_t)r0 * MLP_HIDDEN;
+  for (int r0 = 0; r0 < n; r0 += RB) {
+    const float* xr[RB];
+    for (int k = 0; k < RB; ++k) xr[k] = x + (size_t)std::min(r0 + k, n - 1) * in;
     for (int o0 = 0; o0 < MLP_HIDDEN; o0 += OB) {
-      F4 acc0[NV], acc1[NV];
-      for (int k = 0; k < NV; ++k) acc0[k] = acc1[k] = load4(b + o0 + 4 * k);
+      F4 acc[RB][NV];
+      for (int k = 0; k < RB; ++k)
+        for (int v = 0; v < NV; ++v) acc[k][v] = load4(b + o0 + 4 * v);
       const float* w = wt + o0;
       for (int i = 0; i < in; ++i, w += MLP_HIDDEN) {
-        const F4 a0 = {x0[i], x0[i], x0[i], x0[i]};
-        const F4 a1 = {x1[i], x1[i], x1[i], x1[i]};
-        for (int k = 0; k < NV; ++k) {
-          const F4 wk = load4(w + 4 * k);
-          acc0[k] += a0 * wk;
-          acc1[k] += a1 * wk;
+        F4 wv[NV];
+        for (int v = 0; v < NV; ++v) wv[v] = load4(w + 4 * v);
+        for (int k = 0; k < RB; ++k) {
+          const F4 a = {xr[k][i], xr[k][i], xr[k][i], xr[k][i]};
+          for (int v = 0; v < NV; ++v) acc[k][v] += a * wv[v];
         }
       }
-      for (int k = 0; k < NV; ++k) {
-        const F4 v0 = acc0[k] > zero ? acc0[k] : zero;
-        std::memcpy(y0 + o0 + 4 * k, &v0, sizeof(v0));
-        if (two) {
-          const F4 v1 = acc1[k] > zero ? acc1[k] : zero;
-          std::memcpy(y0 + MLP_HIDDEN + o0 + 4 * k, &v1, sizeof(v1));
+      for (int k = 0; k < RB && r0 + k < n; ++k)
+        for (int v = 0; v < NV; ++v) {
+          const F4 t = acc[k][v] > zero ? acc[k][v] : zero;
+          std::memcpy(y + (size_t)(r0 + k) * MLP_HIDDEN + o0 + 4 * v, &t, sizeof(t));
         }
-      }
     }
   }
 }
