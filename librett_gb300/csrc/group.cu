@@ -177,6 +177,9 @@ struct GroupObj {
   uint64_t signature = 0;
   long long bytes = 0;
   Build built;
+  // Serialises execution against tuning (which rebuilds the graph) and the
+  // introspection calls; creation builds before the group is published.
+  std::mutex mu;
   GroupObj() = default;
   GroupObj(const GroupObj&) = delete;
   GroupObj& operator=(const GroupObj&) = delete;
@@ -590,6 +593,7 @@ librettResult execute(librettGroupHandle h) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   if (dev != g->device) return LIBRETT_INVALID_DEVICE;
+  std::lock_guard<std::mutex> lk(g->mu);
   return launch(*g);
 }
 
@@ -623,6 +627,7 @@ librettResult tune(librettGroupHandle h) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   if (dev != g.device) return LIBRETT_INVALID_DEVICE;
+  std::lock_guard<std::mutex> lk(g.mu);
   long long classBytes[GROUP_CLASSES] = {};
   for (const Member& m : g.members)
     classBytes[m.cls] += 2 * m.plan->pd.f.vol * (long long)m.plan->pd.f.esize;
@@ -678,7 +683,7 @@ librettResult tune(librettGroupHandle h) {
   cudaEventDestroy(e1);
   if (r != LIBRETT_SUCCESS) return r;
   g.tuned = true;
-  std::lock_guard<std::mutex> lk(gTuneMu);
+  std::lock_guard<std::mutex> tk(gTuneMu);
   gTuneCache[g.signature] = cur;
   return LIBRETT_SUCCESS;
 }
@@ -759,6 +764,7 @@ int librett_c_group_info(librettGroupHandle group, int* members, int* buckets, i
                          long long* tiles, long long* bytes) {
   std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
   if (!g) return LIBRETT_INVALID_PLAN;
+  std::lock_guard<std::mutex> lk(g->mu);
   if (members) *members = (int)g->members.size();
   if (buckets) *buckets = g->built.buckets;
   if (separate) *separate = g->built.separate;
@@ -771,6 +777,7 @@ int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int*
                            long long* tiles, long long* bytes) {
   std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
   if (!g) return LIBRETT_INVALID_PLAN;
+  std::lock_guard<std::mutex> lk(g->mu);
   if (index < 0 || index >= (int)g->built.summary.size()) return LIBRETT_INVALID_PARAMETER;
   const lt::BucketSummary& b = g->built.summary[index];
   if (shape) {
@@ -790,6 +797,7 @@ int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int*
 int librett_c_group_policy(librettGroupHandle group, int* policy, int* tuned) {
   std::shared_ptr<lt::GroupObj> g = lt::findGroup(group);
   if (!g) return LIBRETT_INVALID_PLAN;
+  std::lock_guard<std::mutex> lk(g->mu);
   if (policy)
     for (int c = 0; c < lt::GROUP_CLASSES; ++c) policy[c] = g->policy[c];
   if (tuned) *tuned = g->tuned ? 1 : 0;
