@@ -665,7 +665,8 @@ librettResult tune(librettGroupHandle h) {
     std::vector<int> alts;
     for (int t = 0; t < GP_TILES; ++t)
       if (t != tile) alts.push_back(t + GP_TILES * loads);
-    alts.push_back(tile + GP_TILES * (1 - loads));
+    for (int l = 0; l < GP_COUNT / GP_TILES; ++l)
+      if (l != loads) alts.push_back(tile + GP_TILES * l);
     for (int p : alts) {
       Policy pol = cur;
       pol[c] = p;

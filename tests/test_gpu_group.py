@@ -270,3 +270,36 @@ def test_group_errors(cuda):
         with pytest.raises(L.LibrettError) as e:
             L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 12, 0))
         assert e.value.code == L.LIBRETT_INVALID_PARAMETER
+
+
+def test_group_execute_while_tuning(cuda):
+    # one thread executes the group while another tunes it (the tuner
+    # rebuilds the graph); every execution must see a complete graph
+    import threading
+
+    import torch
+
+    probs = _mixed_problems(120, seed=19)
+    b = _Batch(probs, [False] * len(probs), seed=12)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    errors = []
+    with L.Group(plans, ins, outs, stream) as g:
+        def runner():
+            try:
+                for _ in range(50):
+                    g.execute()
+            except Exception as e:  # reported below
+                errors.append(e)
+
+        t = threading.Thread(target=runner)
+        t.start()
+        g.tune()
+        t.join()
+        assert not errors, errors
+        b.out.fill_(CANARY)
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
