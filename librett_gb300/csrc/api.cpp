@@ -433,19 +433,20 @@ int librett_c_group_run_check(int rank, const int* dim, const int* permutation, 
   std::vector<int> ldRow(tp.tileVol / rs.inRun), stRow(tp.tileVol / rs.outRun),
       smRow(tp.tileVol / rs.outRun), smRun(rs.outRun);
   lt::groupRunTablesHost(tp, rs, ldRow.data(), stRow.data(), smRow.data(), smRun.data());
-  const lt::FastDiv inRun = lt::makeFastDiv((uint32_t)rs.inRun);
-  const lt::FastDiv outRun = lt::makeFastDiv((uint32_t)rs.outRun);
+  const lt::RunDiv inRun = lt::makeRunDiv((uint32_t)rs.inRun);
+  const lt::RunDiv outRun = lt::makeRunDiv((uint32_t)rs.outRun);
   auto pad = [&](int j) { return j + ((j >> tp.padShift) << tp.padLog); };
+  if (tp.tileVol >= 65536) return LIBRETT_INTERNAL_ERROR;  // run division needs indices < 2^16
   // the kernel's index arithmetic, unit by unit
   for (int u = 0; u < tp.nIn; ++u) {
     const int j = u * tp.lv;
-    const uint32_t r = lt::fastDivHost((uint32_t)j, inRun);
+    const uint32_t r = lt::runDivHost((uint32_t)j + 1, inRun);
     const int a = j - (int)(r * inRun.d);
     if (r >= ldRow.size() || a + ldRow[r] != ldOff[u]) return LIBRETT_INTERNAL_ERROR;
   }
   for (int w = 0; w < tp.nOut; ++w) {
     const int q = w * tp.sv;
-    const uint32_t r = lt::fastDivHost((uint32_t)q, outRun);
+    const uint32_t r = lt::runDivHost((uint32_t)q + 1, outRun);
     const int a = q - (int)(r * outRun.d);
     if (r >= stRow.size() || a + tp.sv > rs.outRun || a + stRow[r] != stOff[w])
       return LIBRETT_INTERNAL_ERROR;

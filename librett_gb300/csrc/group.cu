@@ -277,6 +277,8 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     out.slots = out.slotsScalar;
     out.smemBytes = out.tile.smStride * out.f.esize;
   }
+  // the kernel's run division needs in-tile indices below 2^16 (RunDiv)
+  if (out.tile.tileVol >= 65536) return false;
   // the tile data plus the staged store-side tables
   out.smemBytes = out.tile.smStride * out.f.esize + stagedTableBytes(out.tile);
   return true;
@@ -400,8 +402,8 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.smRun = reinterpret_cast<const int*>(tb + sub[2]);
       t.nIn = tp.nIn;
       t.nOut = tp.nOut;
-      t.inRun = makeFastDiv((uint32_t)rs.inRun);
-      t.outRun = makeFastDiv((uint32_t)rs.outRun);
+      t.inRun = makeRunDiv((uint32_t)rs.inRun);
+      t.outRun = makeRunDiv((uint32_t)rs.outRun);
       t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
       t.tabBytes = stagedTableBytes(tp);
       t.smRunOff = (int)((sub[2] - sub[1]) / 4);

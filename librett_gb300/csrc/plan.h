@@ -62,6 +62,26 @@ inline uint32_t fastDivHost(uint32_t n, const FastDiv& f) {
   return (uint32_t)(((uint64_t)n * f.mul) >> f.shift);
 }
 
+// Division of in-tile indices (n < 2^16) by run lengths (1 <= d < 2^16)
+// with one multiply-high and no shift: mul = floor((2^32 - 1) / d) and
+// n / d == umulhi(n + 1, mul).  Proof: r = 2^32 - mul * d lies in [1, d], so
+// (n + 1) * mul / 2^32 = (n + 1) / d - (n + 1) * r / (d * 2^32); with
+// n = q * d + t the second term is positive and at most 1 / d whenever
+// (n + 1) * d <= 2^32, so the floor is q for every t in [0, d).  Kernels
+// carry n + 1 instead of n, which folds the increment into the multiply-add
+// that forms the index.
+struct RunDiv {
+  uint32_t d;
+  uint32_t mul;
+};
+
+inline RunDiv makeRunDiv(uint32_t d) { return RunDiv{d, 0xFFFFFFFFu / d}; }
+
+// n / d for n + 1 = n1; exact while n1 * d <= 2^32.
+inline uint32_t runDivHost(uint32_t n1, const RunDiv& f) {
+  return (uint32_t)(((uint64_t)n1 * f.mul) >> 32);
+}
+
 // Problem after dropping unit dims and fusing ranks that stay adjacent under
 // the permutation (the role of LibreTT's reduceRanks, src/plan.cpp:64-127).
 struct Fused {

@@ -19,6 +19,8 @@
 // and only two 64-bit bases change per tile.
 #pragma once
 
+#include <type_traits>
+
 #include "group.h"
 #include "kernels.cuh"
 
@@ -325,6 +327,45 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   storeTile<ES, SV>(p, stOff, stSm, s, out + bout);
 }
 
+// p + i * scale bytes.  With a scale the compiler cannot see (opaque), the
+// offset is one wide integer multiply-add on the FMA pipe instead of a
+// sign extension and a shift-add pair on the ALU pipe, which the grouped
+// kernel's narrow units would otherwise saturate.
+template <typename P>
+__device__ __forceinline__ P* offsetBytes(P* p, int i, int scale) {
+  using B = typename std::conditional<std::is_const<P>::value, const unsigned char,
+                                      unsigned char>::type;
+  return reinterpret_cast<P*>(reinterpret_cast<B*>(p) + (long long)i * scale);
+}
+
+template <int BYTES>
+__device__ __forceinline__ typename Word<BYTES>::T ldShared(uint32_t addr) {
+  typename Word<BYTES>::T v;
+  if constexpr (BYTES == 4) {
+    asm volatile("ld.shared.b32 %0, [%1];\n" : "=r"(v) : "r"(addr));
+  } else if constexpr (BYTES == 8) {
+    asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];\n" : "=r"(v.x), "=r"(v.y) : "r"(addr));
+  } else {
+    asm volatile("ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "r"(addr));
+  }
+  return v;
+}
+
+template <int BYTES>
+__device__ __forceinline__ void stShared(uint32_t addr, const typename Word<BYTES>::T& v) {
+  if constexpr (BYTES == 4) {
+    asm volatile("st.shared.b32 [%0], %1;\n" ::"r"(addr), "r"(v) : "memory");
+  } else if constexpr (BYTES == 8) {
+    asm volatile("st.shared.v2.b32 [%0], {%1, %2};\n" ::"r"(addr), "r"(v.x), "r"(v.y) : "memory");
+  } else {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};\n" ::"r"(addr), "r"(v.x), "r"(v.y),
+                 "r"(v.z), "r"(v.w)
+                 : "memory");
+  }
+}
+
 // Grouped flat kernel: CTA b moves one tile of tensor tileTensor[b] of a
 // bucket; the tile list gives the tensor and the tile's corner offsets, the
 // tensor's descriptor its pointers and run tables.  Unit
@@ -340,6 +381,15 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
 // aligned 16-byte block that holds a byte of the tensor lies in the same
 // memory page as that byte, so these reads stay in mapped memory even where
 // the block extends past the tensor; the bytes outside the run are dropped.
+//
+// Index arithmetic is kept off the ALU pipe where it can be: with element-
+// size units the kernel does little else, and integer adds, shifts and
+// compares issue at half the rate of multiply-adds.  Load slot k of a thread
+// starts at tile element jT + k * B (B = TILE_THREADS * LV).  Padding puts
+// 2^padLog elements after every 2^padShift, with padShift <= 8 <= log2(B) or
+// padShift = 31 (none), so slot k's padded index is padT + k * padStep: one
+// multiply-add per slot.  Byte offsets are multiply-adds by a scale the
+// compiler cannot fold into shifts.
 template <int ES, int LV, int SV, int NL, int LOADS>
 __global__ void __launch_bounds__(TILE_THREADS)
 groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restrict__ tiles) {
@@ -356,8 +406,11 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
   const T* in = reinterpret_cast<const T*>(g->in) + bin;
   T* out = reinterpret_cast<T*>(g->out) + bout;
   const int* ldRow = g->ldRow;
-  const FastDiv inRun = g->inRun;
+  const RunDiv inRun = g->inRun;
   const int nIn = g->nIn, nOut = g->nOut, padShift = g->padShift, padLog = g->padLog;
+  const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
+  const int esR = opaque(ES);
+  const int padMul = 1 << padLog;
   auto pad = [&](int j) { return j + ((j >> padShift) << padLog); };
   if constexpr (LOADS == 2 && LV == 1 && ES < 16) {
     constexpr int CH = 16 / ES;  // elements per 16-byte block
@@ -383,35 +436,39 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
         }
       }
     }
-  } else if constexpr (LOADS >= 1) {
-    const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
-#pragma unroll
-    for (int k = 0; k < NL; ++k) {
-      const int u = threadIdx.x + k * TILE_THREADS;
-      if (u < nIn) {
-        const int j = u * LV;
-        const uint32_t r = fdiv((uint32_t)j, inRun);
-        const int a = j - (int)(r * inRun.d);
-        cpAsyncUnit<ES * LV>(sBase + (uint32_t)pad(j) * ES, in + a + __ldg(ldRow + r));
-      }
-    }
-    cpAsyncWaitAll();
   } else {
-    LT v[NL];
+    constexpr int B = TILE_THREADS * LV;
+    const int jT = threadIdx.x * LV;
+    const int bR = opaque(B);
+    const uint32_t dst0 = sBase + (uint32_t)((jT + (jT >> padShift) * padMul) * esR);
+    const int stepBytes = (B + (B >> padShift) * padMul) * esR;
+    const int uMax = nIn - threadIdx.x;  // slot k is live while k * TILE_THREADS < uMax
+    const int inD = (int)inRun.d;
+    const int four = opaque(4);
+    const int jT1 = jT + 1;
+    const T* inM1 = in - 1;  // indexed by a + 1
+    auto unitSrc = [&](int k) {
+      // j + 1 = k * B + jT + 1; run r = j / inRun, a + 1 = j + 1 - r * inRun
+      const int j1 = k * bR + jT1;
+      const uint32_t r = __umulhi((uint32_t)j1, inRun.mul);
+      const int a1 = j1 - (int)r * inD;
+      const int row = __ldg(offsetBytes(ldRow, (int)r, four));
+      return reinterpret_cast<const LT*>(offsetBytes(offsetBytes(inM1, a1, esR), row, esR));
+    };
+    if constexpr (LOADS >= 1) {
 #pragma unroll
-    for (int k = 0; k < NL; ++k) {
-      const int u = threadIdx.x + k * TILE_THREADS;
-      if (u < nIn) {
-        const int j = u * LV;
-        const uint32_t r = fdiv((uint32_t)j, inRun);
-        const int a = j - (int)(r * inRun.d);
-        v[k] = *reinterpret_cast<const LT*>(in + a + __ldg(ldRow + r));
-      }
-    }
+      for (int k = 0; k < NL; ++k)
+        if (k * TILE_THREADS < uMax)
+          cpAsyncUnit<ES * LV>(dst0 + (uint32_t)(k * stepBytes), unitSrc(k));
+      cpAsyncWaitAll();
+    } else {
+      LT v[NL];
 #pragma unroll
-    for (int k = 0; k < NL; ++k) {
-      const int u = threadIdx.x + k * TILE_THREADS;
-      if (u < nIn) *reinterpret_cast<LT*>(s + pad(u * LV)) = v[k];
+      for (int k = 0; k < NL; ++k)
+        if (k * TILE_THREADS < uMax) v[k] = *unitSrc(k);
+#pragma unroll
+      for (int k = 0; k < NL; ++k)
+        if (k * TILE_THREADS < uMax) stShared<ES * LV>(dst0 + (uint32_t)(k * stepBytes), v[k]);
     }
   }
   if (tabBytes > 0) {
@@ -424,34 +481,48 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
     cpAsyncWaitAll();
   }
   __syncthreads();
-  const FastDiv outRun = g->outRun;
+  const RunDiv outRun = g->outRun;
+  const int outD = (int)outRun.d;
+  const int qT1 = threadIdx.x * SV + 1;
+  T* outM1 = out - 1;  // indexed by a + 1
+  const int bQ = opaque(TILE_THREADS * SV);
+  const int wMax = nOut - threadIdx.x;  // store slot i is live while i * TILE_THREADS < wMax
+  const int padBytes = padMul * esR;
+  // shared address of (unpadded) tile element x
+  auto smAddr = [&](int x) { return sBase + (uint32_t)(x * esR + (x >> padShift) * padBytes); };
+  // nOut <= NL * TILE_THREADS * LV / SV
+  constexpr int NS = (NL * LV + SV - 1) / SV;
+  constexpr int UNROLL = NS <= 16 ? NS : 8;
   auto storeAll = [&](const int2* outRows, const int* smRun) {
-#pragma unroll 4
-    for (int w = threadIdx.x; w < nOut; w += TILE_THREADS) {
-      const int q = w * SV;
-      const uint32_t r = fdiv((uint32_t)q, outRun);
-      const int a = q - (int)(r * outRun.d);
-      const int2 row = outRows[r];
-      T* dst = out + a + row.x;
-      const int jb = row.y;
-      if constexpr (SV == 1) {
-        *dst = s[pad(jb + smRun[a])];
-      } else {
-        T e[SV];
-        if constexpr (SV == 2) {
-          const int2 jr = *reinterpret_cast<const int2*>(smRun + a);
-          e[0] = s[pad(jb + jr.x)];
-          e[1] = s[pad(jb + jr.y)];
+#pragma unroll UNROLL
+    for (int i = 0; i < NS; ++i) {
+      if (i * TILE_THREADS < wMax) {
+        const int q1 = i * bQ + qT1;  // q + 1
+        const uint32_t r = __umulhi((uint32_t)q1, outRun.mul);
+        const int a1 = q1 - (int)r * outD;  // a + 1
+        const int a = a1 - 1;
+        const int2 row = outRows[r];
+        ST* dst = reinterpret_cast<ST*>(offsetBytes(offsetBytes(outM1, a1, esR), row.x, esR));
+        const int jb = row.y;
+        if constexpr (SV == 1) {
+          *dst = ldShared<ES>(smAddr(jb + smRun[a]));
         } else {
-          const int4 jr = *reinterpret_cast<const int4*>(smRun + a);
-          e[0] = s[pad(jb + jr.x)];
-          e[1] = s[pad(jb + jr.y)];
-          e[2] = s[pad(jb + jr.z)];
-          e[3] = s[pad(jb + jr.w)];
+          T e[SV];
+          if constexpr (SV == 2) {
+            const int2 jr = *reinterpret_cast<const int2*>(smRun + a);
+            e[0] = ldShared<ES>(smAddr(jb + jr.x));
+            e[1] = ldShared<ES>(smAddr(jb + jr.y));
+          } else {
+            const int4 jr = *reinterpret_cast<const int4*>(smRun + a);
+            e[0] = ldShared<ES>(smAddr(jb + jr.x));
+            e[1] = ldShared<ES>(smAddr(jb + jr.y));
+            e[2] = ldShared<ES>(smAddr(jb + jr.z));
+            e[3] = ldShared<ES>(smAddr(jb + jr.w));
+          }
+          ST val;
+          __builtin_memcpy(&val, e, sizeof(ST));
+          *dst = val;
         }
-        ST val;
-        __builtin_memcpy(&val, e, sizeof(ST));
-        *reinterpret_cast<ST*>(dst) = val;
       }
     }
   };
