@@ -436,6 +436,11 @@ int librett_c_group_run_check(int rank, const int* dim, const int* permutation, 
   const lt::RunDiv inRun = lt::makeRunDiv((uint32_t)rs.inRun);
   const lt::RunDiv outRun = lt::makeRunDiv((uint32_t)rs.outRun);
   auto pad = [&](int j) { return j + ((j >> tp.padShift) << tp.padLog); };
+  // evenly spaced input runs must match the table they replace
+  const int ldStep = lt::groupLoadStep(tp, rs, (int)sizeofType);
+  if (ldStep >= 0)
+    for (size_t r = 0; r < ldRow.size(); ++r)
+      if (ldRow[r] != (long long)r * ldStep) return LIBRETT_INTERNAL_ERROR;
   if (tp.tileVol >= 65536) return LIBRETT_INTERNAL_ERROR;  // run division needs indices < 2^16
   // the kernel's index arithmetic, unit by unit
   for (int u = 0; u < tp.nIn; ++u) {

@@ -409,6 +409,8 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.smRunOff = (int)((sub[2] - sub[1]) / 4);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
+      const int step = groupLoadStep(tp, rs, m.pd.f.esize);
+      t.ldStepBytes = step < 0 ? -1 : step * m.pd.f.esize;
       GroupTableJob jb;
       std::memset(&jb, 0, sizeof(jb));
       jb.tp = tp;

@@ -45,6 +45,9 @@ struct GroupTensor {
   // device memory) and the int offset of smRun inside them (outRows first).
   int tabBytes, smRunOff;
   int padShift, padLog;
+  // input run r starts at r * ldStepBytes bytes from the tile corner when
+  // >= 0 (evenly spaced runs; ldRow is then not read), else at ldRow[r]
+  int ldStepBytes;
 };
 
 // One tile of a bucket, written on the device at group creation: the

@@ -260,6 +260,21 @@ GroupRunSplit groupRunSplit(const TileParams& tp) {
   return rs;
 }
 
+int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize) {
+  long long step = 0;
+  int prev = -1;
+  for (int t = rs.kIn; t < tp.nTR; ++t) {
+    if (tp.trE[t] <= 1) continue;
+    if (prev < 0)
+      step = tp.trSin[t];
+    else if ((long long)tp.trSin[t] != (long long)tp.trE[prev] * tp.trSin[prev])
+      return -1;
+    prev = t;
+  }
+  if (step * esize > 0x7fffffffLL) return -1;
+  return (int)step;
+}
+
 void groupRunTablesHost(const TileParams& tp, const GroupRunSplit& rs, int* ldRow, int* stRow,
                         int* smRow, int* smRun) {
   for (int r = 0; r < tp.tileVol / rs.inRun; ++r) {

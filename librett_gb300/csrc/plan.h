@@ -229,6 +229,13 @@ struct GroupRunSplit {
 };
 GroupRunSplit groupRunSplit(const TileParams& tp);
 
+// Step s with ldRow[r] == r * s for every input run r of the tile (the tile
+// ranks after the run chain: each non-unit rank's input stride is the
+// previous one's extent times its stride), so a kernel can form the run's
+// offset without the table; -1 when the runs are not evenly spaced or
+// s * esize does not fit an int.
+int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize);
+
 // Host copy of the run tables: ldRow[tileVol / inRun] input offset of each
 // input run; stRow / smRow[tileVol / outRun] output offset and in-tile
 // (input-order) index of each output run's first element; smRun[outRun]

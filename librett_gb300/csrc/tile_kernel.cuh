@@ -447,29 +447,42 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
     const int four = opaque(4);
     const int jT1 = jT + 1;
     const T* inM1 = in - 1;  // indexed by a + 1
-    auto unitSrc = [&](int k) {
-      // j + 1 = k * B + jT + 1; run r = j / inRun, a + 1 = j + 1 - r * inRun
-      const int j1 = k * bR + jT1;
-      const uint32_t r = __umulhi((uint32_t)j1, inRun.mul);
-      const int a1 = j1 - (int)r * inD;
-      const int row = __ldg(offsetBytes(ldRow, (int)r, four));
-      return reinterpret_cast<const LT*>(offsetBytes(offsetBytes(inM1, a1, esR), row, esR));
+    const int ldStepB = g->ldStepBytes;
+    // STEP: input runs evenly spaced (no table read on the load path)
+    auto loadAll = [&](auto step) {
+      constexpr bool STEP = decltype(step)::value;
+      auto unitSrc = [&](int k) {
+        // j + 1 = k * B + jT + 1; run r = j / inRun, a + 1 = j + 1 - r * inRun
+        const int j1 = k * bR + jT1;
+        const uint32_t r = __umulhi((uint32_t)j1, inRun.mul);
+        const int a1 = j1 - (int)r * inD;
+        const T* runBase;
+        if constexpr (STEP)
+          runBase = offsetBytes(inM1, (int)r, ldStepB);
+        else
+          runBase = offsetBytes(inM1, __ldg(offsetBytes(ldRow, (int)r, four)), esR);
+        return reinterpret_cast<const LT*>(offsetBytes(runBase, a1, esR));
+      };
+      if constexpr (LOADS >= 1) {
+#pragma unroll
+        for (int k = 0; k < NL; ++k)
+          if (k * TILE_THREADS < uMax)
+            cpAsyncUnit<ES * LV>(dst0 + (uint32_t)(k * stepBytes), unitSrc(k));
+        cpAsyncWaitAll();
+      } else {
+        LT v[NL];
+#pragma unroll
+        for (int k = 0; k < NL; ++k)
+          if (k * TILE_THREADS < uMax) v[k] = *unitSrc(k);
+#pragma unroll
+        for (int k = 0; k < NL; ++k)
+          if (k * TILE_THREADS < uMax) stShared<ES * LV>(dst0 + (uint32_t)(k * stepBytes), v[k]);
+      }
     };
-    if constexpr (LOADS >= 1) {
-#pragma unroll
-      for (int k = 0; k < NL; ++k)
-        if (k * TILE_THREADS < uMax)
-          cpAsyncUnit<ES * LV>(dst0 + (uint32_t)(k * stepBytes), unitSrc(k));
-      cpAsyncWaitAll();
-    } else {
-      LT v[NL];
-#pragma unroll
-      for (int k = 0; k < NL; ++k)
-        if (k * TILE_THREADS < uMax) v[k] = *unitSrc(k);
-#pragma unroll
-      for (int k = 0; k < NL; ++k)
-        if (k * TILE_THREADS < uMax) stShared<ES * LV>(dst0 + (uint32_t)(k * stepBytes), v[k]);
-    }
+    if (ldStepB >= 0)
+      loadAll(std::true_type{});
+    else
+      loadAll(std::false_type{});
   }
   if (tabBytes > 0) {
     // the store-side tables (outRows and smRun are contiguous, 16-byte
