@@ -28,6 +28,10 @@ SOURCES = ["api.cpp", "plan.cpp", "select.cpp", "k_misc.cu", "k_tile4.cu", "k_ti
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
           f"-I{INCLUDE}", f"-I{CSRC}"]
+# Host inference of the plan selector: let the compiler fuse its vector
+# multiply-adds (ISO C++ mode turns contraction off; on Arm hosts this halves
+# the instructions of the network's dense layers).
+FILE_FLAGS = {"select.cpp": ["-Xcompiler", "-ffp-contract=fast"]}
 
 
 def nvcc() -> str:
@@ -49,7 +53,8 @@ def _compile(src: str, force: bool, verbose: bool, extra: list[str]) -> Path:
     if (not force and obj.exists()
             and obj.stat().st_mtime >= max(srcp.stat().st_mtime, _headers_mtime())):
         return obj
-    cmd = [nvcc(), *ARCH, *COMMON, *extra, "-c", str(srcp), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *COMMON, *FILE_FLAGS.get(src, []), *extra, "-c", str(srcp), "-o",
+           str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)

@@ -152,13 +152,22 @@ bool offsetsFit(const Fused& f, const int64_t* e) {
 // 60% of it; else equal chunks.
 int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
   int64_t lo = std::max(std::max(cur + 1, (want * 3 + 4) / 5), want - 95);
-  for (int pass = 0; pass < 2; ++pass) {
+  // one descending scan: the first divisor that is a multiple of V (when
+  // that is preferred), else the first divisor
+  const bool preferV = V > 1 && d % V == 0;
+  int64_t firstDiv = 0;
+  auto scan = [&](auto dd) -> int64_t {
+    using U = decltype(dd);
     for (int64_t c = want; c >= lo; --c) {
-      if (d % c != 0) continue;
-      if (pass == 0 && V > 1 && d % V == 0 && c % V != 0) continue;
-      return c;
+      if (dd % (U)c != 0) continue;
+      if (!preferV || c % V == 0) return c;
+      if (firstDiv == 0) firstDiv = c;
     }
-  }
+    return 0;
+  };
+  const int64_t hit = d <= 0xffffffffLL ? scan((uint32_t)d) : scan((uint64_t)d);
+  if (hit != 0) return hit;
+  if (firstDiv != 0) return firstDiv;
   int64_t nch = ceilDiv(d, want);
   int64_t e = ceilDiv(d, nch);
   if (V > 1 && d % V == 0 && e % V != 0) {
@@ -340,16 +349,20 @@ long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
 std::vector<int> storeSample(const TileParams& tp, int sampleUnits, int& n) {
   n = std::min(tp.nOut, sampleUnits);
   std::vector<int> j((size_t)n * tp.sv);
-  for (int m = 0; m < tp.sv; ++m)
-    for (int w = 0; w < n; ++w) {
-      int rem = w * tp.sv + m, jj = 0;
+  // output-order elements q = w * sv + m in sequence: a mixed-radix counter
+  // over the tile ranks in output order carries the input-order index
+  int digit[MAXR] = {};
+  int jj = 0;
+  for (int w = 0; w < n; ++w)
+    for (int m = 0; m < tp.sv; ++m) {
+      j[(size_t)m * n + w] = jj;
       for (int i = 0; i < tp.nTR; ++i) {
         const int t = tp.trOut[i];
-        const int c = rem % tp.trE[t];
-        rem /= tp.trE[t];
-        jj += c * tp.trInTile[t];
+        jj += tp.trInTile[t];
+        if (++digit[i] < tp.trE[t]) break;
+        jj -= tp.trE[t] * tp.trInTile[t];
+        digit[i] = 0;
       }
-      j[(size_t)m * n + w] = jj;
     }
   return j;
 }
