@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "kernels.cuh"
@@ -197,6 +198,151 @@ cudaError_t tablePool(cudaMemPool_t* pool) {
   return cudaSuccess;
 }
 
+// Plan tables come from a host-side suballocator, so that planning makes no
+// device allocation call (a stream-ordered pool allocation costs about as
+// much as the table-writing launch itself).  Per device, blocks of
+// 4 KiB << c bytes (c < TABLE_CLASSES) are carved from 8 MiB slabs
+// (cudaMalloc, kept until the process exits); larger tables come from the
+// pool above.  Reuse is stream-ordered, as with cudaFreeAsync: a free
+// records the block's event on the plan's stream; a plan on the same stream
+// takes the block as it is (stream order puts its table writes after every
+// kernel that read the old tables), a plan on another stream makes its
+// stream wait for that event first.  Blocks freed on the requesting stream
+// are preferred, then unused slab space, so the wait is only paid when there
+// are neither.  A block freed while its stream is being captured leaves
+// circulation; a stream being captured takes no other stream's block.
+constexpr int TABLE_CLASSES = 9;  // 4 KiB .. 1 MiB
+constexpr size_t TABLE_SLAB = 8u << 20;
+
+struct TableBlock {
+  void* p = nullptr;
+  int device = 0;
+  int cls = -1;                   // -1: from the pool
+  cudaStream_t stream = nullptr;  // while free: the stream it was freed on
+  cudaEvent_t freed = nullptr;    // recorded there at the free
+};
+
+struct TableArena {
+  std::mutex mu;
+  std::unordered_map<void*, TableBlock*> blocks;  // handed out or free
+  struct Dev {
+    std::vector<TableBlock*> freeBlocks[TABLE_CLASSES];
+    char* cur = nullptr;
+    size_t left = 0;
+  };
+  std::map<int, Dev> devs;
+};
+
+TableArena& tableArena() {
+  static TableArena* a = new TableArena();  // lives until the process exits
+  return *a;
+}
+
+cudaError_t tableAlloc(size_t bytes, cudaStream_t s, void** out) {
+  *out = nullptr;
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  int c = 0;
+  while (c < TABLE_CLASSES && (size_t(4096) << c) < bytes) ++c;
+  TableArena& A = tableArena();
+  if (c == TABLE_CLASSES) {
+    cudaMemPool_t pool = nullptr;
+    err = tablePool(&pool);
+    if (err == cudaSuccess) err = cudaMallocFromPoolAsync(out, bytes, pool, s);
+    if (err != cudaSuccess) return err;
+    TableBlock* b = new TableBlock();
+    b->p = *out;
+    b->device = dev;
+    std::lock_guard<std::mutex> lk(A.mu);
+    A.blocks[b->p] = b;
+    return cudaSuccess;
+  }
+  const size_t size = size_t(4096) << c;
+  // a captured stream cannot wait on an event recorded outside the capture
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  const bool canWait =
+      cudaStreamIsCapturing(s, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone;
+  for (;;) {
+    TableBlock* other = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(A.mu);
+      TableArena::Dev& D = A.devs[dev];
+      std::vector<TableBlock*>& fl = D.freeBlocks[c];
+      for (size_t i = fl.size(); i-- > 0;) {
+        if (fl[i]->stream != s) continue;
+        TableBlock* b = fl[i];
+        fl.erase(fl.begin() + (std::ptrdiff_t)i);
+        *out = b->p;
+        return cudaSuccess;
+      }
+      if (D.left >= size) {
+        TableBlock* b = new TableBlock();
+        b->p = D.cur;
+        b->device = dev;
+        b->cls = c;
+        D.cur += size;
+        D.left -= size;
+        A.blocks[b->p] = b;
+        *out = b->p;
+        return cudaSuccess;
+      }
+      if (canWait && !fl.empty()) {
+        other = fl.front();  // the longest-freed block of another stream
+        fl.erase(fl.begin());
+      }
+    }
+    if (other != nullptr) {
+      err = cudaStreamWaitEvent(s, other->freed, 0);
+      if (err == cudaSuccess) {
+        *out = other->p;
+        return cudaSuccess;
+      }
+      std::lock_guard<std::mutex> lk(A.mu);  // not usable from s: back to the list
+      A.devs[dev].freeBlocks[c].push_back(other);
+      return err;
+    }
+    // a new slab (outside the lock: cudaMalloc may wait for the device)
+    void* slab = nullptr;
+    err = cudaMalloc(&slab, TABLE_SLAB);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> lk(A.mu);
+    TableArena::Dev& D = A.devs[dev];
+    D.cur = static_cast<char*>(slab);
+    D.left = TABLE_SLAB;
+  }
+}
+
+void tableFree(void* p, cudaStream_t s) {
+  if (p == nullptr) return;
+  TableArena& A = tableArena();
+  TableBlock* b = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(A.mu);
+    auto it = A.blocks.find(p);
+    if (it == A.blocks.end()) return;
+    b = it->second;
+    if (b->cls < 0) A.blocks.erase(it);
+  }
+  if (b->cls < 0) {
+    delete b;
+    cudaFreeAsync(p, s);
+    return;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone ||
+      (b->freed == nullptr &&
+       cudaEventCreateWithFlags(&b->freed, cudaEventDisableTiming) != cudaSuccess) ||
+      cudaEventRecord(b->freed, s) != cudaSuccess) {
+    std::lock_guard<std::mutex> lk(A.mu);
+    A.blocks.erase(p);  // leaves circulation
+    return;
+  }
+  b->stream = s;
+  std::lock_guard<std::mutex> lk(A.mu);
+  A.devs[b->device].freeBlocks[b->cls].push_back(b);
+}
+
 cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt) {
   *alloc = nullptr;
   *dt = DeviceTables();
@@ -204,15 +350,12 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
   size_t stOffset, smOffset;
   const size_t total = deviceTableBytes(pd.tile, &stOffset, &smOffset);
   void* d = nullptr;
-  cudaMemPool_t pool = nullptr;
-  cudaError_t err = tablePool(&pool);
-  if (err != cudaSuccess) return err;
-  err = cudaMallocFromPoolAsync(&d, total, pool, s);
+  cudaError_t err = tableAlloc(total, s, &d);
   if (err != cudaSuccess) return err;
   // the tables are computed on the device, in stream order before any use
   err = writeDeviceTables(pd.tile, static_cast<unsigned char*>(d), s, dt);
   if (err != cudaSuccess) {
-    cudaFreeAsync(d, s);
+    tableFree(d, s);
     *dt = DeviceTables();
     return err;
   }
@@ -220,9 +363,7 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
   return cudaSuccess;
 }
 
-void destroyDeviceTables(void* alloc, cudaStream_t s) {
-  if (alloc != nullptr) cudaFreeAsync(alloc, s);
-}
+void destroyDeviceTables(void* alloc, cudaStream_t s) { tableFree(alloc, s); }
 
 cudaError_t launchPlan(const PlanDesc& pd, const DeviceTables* dt, const void* in, void* out,
                        cudaStream_t s, int numSMs, int* grid) {

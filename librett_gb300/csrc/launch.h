@@ -15,12 +15,13 @@ struct DeviceTables {
   const unsigned short* stSm = nullptr;
 };
 
-// Allocates the plan's tables stream-ordered on s (from the library's
-// per-device table pool) and writes them with a kernel on s.  Plans of other
+// Allocates the plan's tables (from the library's per-device table arena,
+// stream-ordered reuse) and writes them with a kernel on s.  Plans of other
 // pipelines need none: *alloc = nullptr.
 cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt);
 
-// Releases them in stream order (cudaFreeAsync on s).
+// Releases them in stream order: reusable at once by plans on s, by plans on
+// other streams once s has passed this point.
 void destroyDeviceTables(void* alloc, cudaStream_t s);
 
 // Device-table layout of a tile: total bytes; ldOff at 0, stOff at
