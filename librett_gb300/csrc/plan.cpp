@@ -329,6 +329,35 @@ long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
   long long cost = 0;
   const int lanesPerPhase = std::max(1, 32 / wordsPerLane);
   for (int ph = 0; ph < 32; ph += lanesPerPhase) {
+    // Closed form for an arithmetic progression of start words over the
+    // phase's active lanes (all of them, or a prefix), stride s: lanes l and
+    // l' share a start bank iff (l - l') * s == 0 mod 32, i.e. iff
+    // P = 32 / g divides l - l' (g = gcd(s, 32), a power of two); distinct
+    // start banks are at least g apart, so with wordsPerLane <= g no two
+    // lanes' word ranges overlap across start banks, and the busiest bank
+    // holds ceil(L / P) words of the L lanes.
+    int L = 0;
+    while (L < lanesPerPhase && act[ph + L]) ++L;
+    bool prefix = true;
+    for (int l = ph + L; l < ph + lanesPerPhase && prefix; ++l) prefix = !act[l];
+    if (prefix && L <= 1) {
+      cost += L;
+      continue;
+    }
+    if (prefix) {
+      const int s = addr[ph + 1] - addr[ph];
+      bool ap = true;
+      for (int l = ph + 2; l < ph + L && ap; ++l) ap = addr[l] - addr[l - 1] == s;
+      if (ap) {
+        const int sm = s & 31;
+        const int g = sm == 0 ? 32 : (sm & -sm);  // gcd(s, 32)
+        if (wordsPerLane <= g) {
+          const int P = 32 / g;
+          cost += (L + P - 1) / P;
+          continue;
+        }
+      }
+    }
     unsigned char cnt[32] = {};
     int maxPerBank = 0;
     for (int l = ph; l < ph + lanesPerPhase; ++l) {
