@@ -321,13 +321,15 @@ bool loadSelectorModel(const char* path, std::string* why) {
   return true;
 }
 
-// Candidates the learned model ranks: the analytic model's cheapest few.  On
-// the held-out timings a short list of 3 keeps the choice within 0.2% of
-// ranking every candidate while the network runs on less than half of them.
+// Candidates the learned model ranks: the analytic model's cheapest few.  A
+// short list of 4 (one block of the batched forward) costs no measurable
+// throughput against ranking every candidate (random-shape suite geomean
+// 6399.5 vs 6399.0 GB/s on one GB300, held-out regret 1.53% vs 1.43%), while
+// the network runs on about half of them; 3 cost 0.5% on the suite.
 int shortlistSize() {
   static const int k = [] {
     const char* e = std::getenv("LIBRETT_SELECTOR_SHORTLIST");
-    const int v = e != nullptr && *e ? std::atoi(e) : 3;
+    const int v = e != nullptr && *e ? std::atoi(e) : 4;
     return v > 0 ? v : 1 << 30;  // 0: every candidate
   }();
   return k;

@@ -114,7 +114,7 @@ def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selec
 
 
 def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore_selector):
-    """The analytic model short-lists its 3 cheapest candidates (ties by
+    """The analytic model short-lists its 4 cheapest candidates (ties by
     index); the learned pick is the lowest prediction among those."""
     lib = restore_selector
     path, params = _write(tmp_path, sms=152)
@@ -125,7 +125,7 @@ def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore
         X = np.stack([D.features(dims, perm, es, c) for c in range(n)])
         pred, _ = M.forward(params, X)
         cost = [L.describe(dims, perm, es, candidate=c)["model_cost"] for c in range(n)]
-        short = sorted(range(n), key=lambda c: cost[c])[:3]
+        short = sorted(range(n), key=lambda c: cost[c])[:4]
         got = L.describe(dims, perm, es)["candidate"]
         assert got in short
         best = pred[short].min()
