@@ -140,6 +140,21 @@ class GpuMlp:
         return self.p.cpu().numpy().copy()
 
 
+def predict_host(params, Xs):
+    """The library's host inference (the planner's own), for standardised
+    rows Xs."""
+    lib = _lib.load()
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(Xs, dtype=np.float32)
+    out = np.zeros(x.shape[0], dtype=np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    rc = lib.librett_c_mlp_predict_host(p.ctypes.data_as(fp), x.ctypes.data_as(fp), x.shape[0],
+                                        out.ctypes.data_as(fp))
+    if rc != 0:
+        raise RuntimeError(f"librett_c_mlp_predict_host: {rc}")
+    return out
+
+
 def predict_gpu(params, Xs, batch=4096):
     import torch
 
@@ -198,17 +213,72 @@ def geo_regret(reg):
     return float(np.exp(np.mean(np.log1p(reg))) - 1.0)
 
 
+# Feature columns (librett_gb300/csrc/select.cpp planFeatures): 9 and 10 mark
+# the persistent pipelines, which are not in the default candidate set; 30 is
+# the analytic model's cost (log scale, monotone in it).
+PIPE_REG_COL, PIPE_ASYNC_COL, COST_COL = 9, 10, 30
+
+
+def shortlist_regret(score, X, t, prob, k):
+    """Regret of the deployed selection, per problem: within the default
+    candidate set, the lowest score among the analytic model's k cheapest
+    candidates (k <= 0: among all), against the set's measured best."""
+    default = (X[:, PIPE_REG_COL] == 0) & (X[:, PIPE_ASYNC_COL] == 0)
+    reg = []
+    for p in np.unique(prob):
+        m = np.nonzero((prob == p) & default)[0]
+        if len(m) == 0:
+            continue
+        keep = m[np.argsort(X[m, COST_COL], kind="stable")]
+        if k > 0:
+            keep = keep[:k]
+        pick = keep[np.argmin(score[keep])]
+        reg.append(t[pick] / t[m].min() - 1.0)
+    return np.array(reg)
+
+
+def evaluate_model(d, model, holdout):
+    """Held-out and training regret of a saved model on a dataset, with the
+    planner's short lists (host inference, no GPU needed)."""
+    X, t, prob = d["X"], d["t"], d["prob"]
+    split = int(prob.max()) + 1 - holdout
+    pred = predict_host(model["params"], (X - model["mean"]) / model["std"])
+    rep = {}
+    for name, mask in (("train", prob < split), ("holdout", prob >= split)):
+        r = {}
+        for k in (0, 4, 3):
+            reg = shortlist_regret(pred[mask], X[mask], t[mask], prob[mask], k)
+            r[f"shortlist_{k or 'all'}"] = {"geomean_regret": geo_regret(reg),
+                                             "p90_regret": float(np.quantile(reg, 0.9)),
+                                             "problems": int(len(reg))}
+        rep[name] = r
+    return rep
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--data", required=True)
     ap.add_argument("--holdout", type=int, default=1000, help="last N problems are held out")
     ap.add_argument("--epochs", type=int, default=60)
-    ap.add_argument("--out", required=True)
+    ap.add_argument("--out", default=None)
     ap.add_argument("--report", default=None)
+    ap.add_argument("--evaluate", default=None, metavar="MODEL",
+                    help="no training: report the regret of this saved model over the default "
+                         "candidate set, ranking all candidates or the analytic short list of 4 "
+                         "or 3 (host inference)")
     ap.add_argument("--extra", action="append", default=[],
                     help="further datasets used for training only (e.g. larger problems)")
     args = ap.parse_args(argv)
     d = np.load(args.data)
+    if args.evaluate:
+        rep = evaluate_model(d, load_model(args.evaluate), args.holdout)
+        print(json.dumps(rep, indent=1))
+        if args.report:
+            with open(args.report, "w") as f:
+                json.dump(rep, f, indent=1)
+        return 0
+    if args.out is None:
+        ap.error("--out is required when training")
     X, t, prob, cand = d["X"], d["t"], d["prob"], d["cand"]
     heur = d["heuristic"]
     nprob = int(prob.max()) + 1

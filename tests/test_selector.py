@@ -132,6 +132,21 @@ def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore
         assert pred[got] <= best + 1e-4 * max(1.0, abs(best))
 
 
+def test_shortlist_regret_rules():
+    """Deployed-selection regret: persistent-pipeline candidates are outside
+    the default set, the short list is the k lowest analytic costs, the pick
+    the lowest score on it, regret against the set's best."""
+    X = np.zeros((5, NF), dtype=np.float32)
+    X[:, T.COST_COL] = [0.1, 0.2, 0.3, 0.4, 0.0]
+    X[4, T.PIPE_REG_COL] = 1  # cheapest and fastest, but not a default candidate
+    t = np.array([3.0, 2.0, 1.5, 1.0, 0.5])
+    prob = np.zeros(5, dtype=int)
+    score = np.array([5.0, 4.0, 3.0, 0.0, -1.0])
+    assert T.shortlist_regret(score, X, t, prob, 0)[0] == 0.0  # picks candidate 3
+    assert T.shortlist_regret(score, X, t, prob, 3)[0] == 0.5  # 2 of {0, 1, 2}: 1.5 / 1.0
+    assert T.shortlist_regret(score, X, t, prob, 1)[0] == 2.0  # only 0: 3.0 / 1.0
+
+
 def test_targets_relative_and_clipped():
     t = np.array([1.0, 2.0, 100.0, 3.0, 3.0])
     prob = np.array([0, 0, 0, 1, 1])
