@@ -177,6 +177,84 @@ __device__ __forceinline__ void storeTile(const TileParams& p, const int* __rest
   }
 }
 
+// Shared indices of store unit w's SV elements (stSm entries) in one word.
+template <int SV> struct SmIdx;
+template <> struct SmIdx<1> { using T = unsigned short; };
+template <> struct SmIdx<2> { using T = unsigned; };
+template <> struct SmIdx<4> { using T = uint2; };
+
+template <int SV>
+__device__ __forceinline__ typename SmIdx<SV>::T loadSmIdx(const unsigned short* __restrict__ stSm,
+                                                           int w) {
+  return __ldg(reinterpret_cast<const typename SmIdx<SV>::T*>(stSm + SV * w));
+}
+
+// Store unit w: gathers its SV elements at shared indices idx and writes
+// them as one access at dst.
+template <int ES, int SV>
+__device__ __forceinline__ void storeUnit(const typename Word<ES>::T* s,
+                                          typename SmIdx<SV>::T idx, typename Word<ES>::T* dst) {
+  using T = typename Word<ES>::T;
+  using ST = typename Word<ES * SV>::T;
+  if constexpr (SV == 1) {
+    *dst = s[idx];
+  } else {
+    T e[SV];
+    if constexpr (SV == 2) {
+      e[0] = s[idx & 0xffffu];
+      e[1] = s[idx >> 16];
+    } else {
+      e[0] = s[idx.x & 0xffffu];
+      e[1] = s[idx.x >> 16];
+      e[2] = s[idx.y & 0xffffu];
+      e[3] = s[idx.y >> 16];
+    }
+    ST v;
+    __builtin_memcpy(&v, e, sizeof(ST));
+    *reinterpret_cast<ST*>(dst) = v;
+  }
+}
+
+// Table entries of a thread's first store units, fetched while the tile's
+// data loads are in flight so that the stores can start as soon as the
+// barrier opens: the tables are a dependent device-memory read otherwise.
+template <int SV, int PF>
+struct StorePrefetch {
+  int off[PF > 0 ? PF : 1];
+  typename SmIdx<SV>::T idx[PF > 0 ? PF : 1];
+
+  __device__ __forceinline__ void load(const TileParams& p, const int* __restrict__ stOff,
+                                       const unsigned short* __restrict__ stSm) {
+#pragma unroll
+    for (int i = 0; i < PF; ++i) {
+      const int w = threadIdx.x + i * TILE_THREADS;
+      if (w < p.nOut) {
+        off[i] = __ldg(stOff + w);
+        idx[i] = loadSmIdx<SV>(stSm, w);
+      }
+    }
+  }
+};
+
+// Store phase of the flat pipeline: the prefetched units first, then the
+// rest as in storeTile.
+template <int ES, int SV, int PF>
+__device__ __forceinline__ void storeTileFlat(const TileParams& p, const int* __restrict__ stOff,
+                                              const unsigned short* __restrict__ stSm,
+                                              const StorePrefetch<SV, PF>& pf,
+                                              const typename Word<ES>::T* s,
+                                              typename Word<ES>::T* outBase) {
+#pragma unroll
+  for (int i = 0; i < PF; ++i) {
+    const int w = threadIdx.x + i * TILE_THREADS;
+    if (w < p.nOut) storeUnit<ES, SV>(s, pf.idx[i], outBase + pf.off[i]);
+  }
+  const int tv = opaque(threadIdx.x);
+#pragma unroll 4
+  for (int w = tv + PF * TILE_THREADS; w < p.nOut; w += TILE_THREADS)
+    storeUnit<ES, SV>(s, loadSmIdx<SV>(stSm, w), outBase + stOff[w]);
+}
+
 // Register-staged pipeline: load units go global -> registers -> shared
 // memory; the next tile's loads are issued before the current tile's
 // stores.  Two shared data buffers, one barrier per tile.
@@ -298,6 +376,12 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   T* s = reinterpret_cast<T*>(smraw);
   long long bin, bout;
   decodeTile(p, blockIdx.x, bin, bout);
+  // store units per thread: nOut <= NL * TILE_THREADS * LV / SV; up to two
+  // are prefetched, except where the register pipeline already holds
+  // NL >= 4 data words (measured slower there: C3b 2 % down)
+  constexpr int NS = (NL * LV + SV - 1) / SV;
+  constexpr int PF_MAX = (NL >= LT_FLAT_ASYNC_MIN_NL || NL < 4) ? 2 : 0;
+  StorePrefetch<SV, NS < PF_MAX ? NS : PF_MAX> pf;
   if constexpr (NL >= LT_FLAT_ASYNC_MIN_NL) {
     // many load units per thread: cp.async straight into shared memory
     // instead of NL data registers per thread
@@ -309,6 +393,7 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
         cpAsyncUnit<ES * LV>(sBase + (uint32_t)smemIndex(p, u * LV) * ES,
                              in + bin + __ldg(ldOff + u));
     }
+    pf.load(p, stOff, stSm);
     cpAsyncWaitAll();
   } else {
     LT v[NL];
@@ -317,6 +402,7 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
       const int u = threadIdx.x + k * TILE_THREADS;
       if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + __ldg(ldOff + u));
     }
+    pf.load(p, stOff, stSm);
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int u = threadIdx.x + k * TILE_THREADS;
@@ -324,7 +410,7 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
     }
   }
   __syncthreads();
-  storeTile<ES, SV>(p, stOff, stSm, s, out + bout);
+  storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
 }
 
 // p + i * scale bytes.  With a scale the compiler cannot see (opaque), the
