@@ -424,6 +424,50 @@ __device__ __forceinline__ P* offsetBytes(P* p, int i, int scale) {
   return reinterpret_cast<P*>(reinterpret_cast<B*>(p) + (long long)i * scale);
 }
 
+// cp.async of one unit, issued only where live: the guard is a predicate on
+// the instruction rather than a branch around it (the compiler cannot
+// if-convert inline assembly, so a guarded asm costs a branch per slot).
+template <int BYTES>
+__device__ __forceinline__ void cpAsyncUnitIf(bool live, uint32_t dst, const void* src) {
+  static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async unit");
+  if constexpr (BYTES == 16)
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %2, 0;\n"
+        " @p cp.async.cg.shared.global [%0], [%1], 16;\n}\n" ::"r"(dst),
+        "l"(src), "r"((int)live)
+        : "memory");
+  else
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %3, 0;\n"
+        " @p cp.async.ca.shared.global [%0], [%1], %2;\n}\n" ::"r"(dst),
+        "l"(src), "n"(BYTES), "r"((int)live)
+        : "memory");
+}
+
+// Shared load where live (predicated as above); the result is undefined
+// where not live.
+template <int BYTES>
+__device__ __forceinline__ typename Word<BYTES>::T ldSharedIf(bool live, uint32_t addr) {
+  typename Word<BYTES>::T v;
+  if constexpr (BYTES == 4) {
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %2, 0;\n @p ld.shared.b32 %0, [%1];\n}\n"
+                 : "=r"(v)
+                 : "r"(addr), "r"((int)live));
+  } else if constexpr (BYTES == 8) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %3, 0;\n @p ld.shared.v2.b32 {%0, %1}, [%2];\n}\n"
+        : "=r"(v.x), "=r"(v.y)
+        : "r"(addr), "r"((int)live));
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+        " @p ld.shared.v4.b32 {%0, %1, %2, %3}, [%4];\n}\n"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "r"(addr), "r"((int)live));
+  }
+  return v;
+}
+
 template <int BYTES>
 __device__ __forceinline__ typename Word<BYTES>::T ldShared(uint32_t addr) {
   typename Word<BYTES>::T v;
@@ -552,7 +596,10 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
       if constexpr (LOADS >= 1) {
 #pragma unroll
         for (int k = 0; k < NL; ++k)
-          if (k * TILE_THREADS < uMax)
+          if constexpr (STEP)  // the source is arithmetic only: predicate the copy
+            cpAsyncUnitIf<ES * LV>(k * TILE_THREADS < uMax, dst0 + (uint32_t)(k * stepBytes),
+                                   unitSrc(k));
+          else if (k * TILE_THREADS < uMax)  // a dead slot's run would index past ldRow
             cpAsyncUnit<ES * LV>(dst0 + (uint32_t)(k * stepBytes), unitSrc(k));
         cpAsyncWaitAll();
       } else {
