@@ -224,6 +224,7 @@ def cpu_gather_time(problems, budget_s, threads, rng_seed=1):
 
 
 GROUP_SLICE = 100  # problems per reference-arm step of the grouped workload
+E2E_CHUNKS = 4  # groups the grouped end-to-end prefix is cut into for copy overlap
 
 
 def _reference_grouped(args, problems, threads):
@@ -423,19 +424,50 @@ def run_engine(args):
                                 for p, t in zip(problems, per_problem_ms)])))
     ceiling = copy_ceiling(inp, out, stream, (maxb // 8) * 8) if maxb >= 1 << 26 else None
 
-    # end to end through the public API: pinned host in -> device -> host out
+    # end to end through the public API: pinned host in -> device -> host out.
+    # The problems stream through two device buffer pairs: problem i + 1's
+    # input copy (its own stream), problem i's transpose (the plans' stream)
+    # and problem i - 1's result copy (a third stream) overlap, the two
+    # copies in opposite directions of the host link.
     e2e = None
     if not args.no_e2e:
         hin = torch.empty(maxb, dtype=torch.uint8, pin_memory=True)
         hin.copy_(inp.cpu())
         hout = torch.empty(maxb, dtype=torch.uint8, pin_memory=True)
+        d_in = [inp, torch.empty_like(inp)]
+        d_out = [out, torch.empty_like(out)]
+        s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+        torch.cuda.synchronize(dev)
 
         def e2e_step():
-            for (dims, perm, es), pl in zip(problems, plans):
-                nb = problem_bytes((dims, perm, es))
-                inp[:nb].copy_(hin[:nb], non_blocking=True)
-                pl.execute(ip, op)
-                hout[:nb].copy_(out[:nb], non_blocking=True)
+            start = torch.cuda.Event()
+            start.record(stream)
+            s_in.wait_event(start)
+            s_out.wait_event(start)
+            loaded = [torch.cuda.Event() for _ in range(2)]
+            done = [None, None]  # transpose of the buffer pair finished
+            saved = [None, None]  # its result copied back
+            for i, ((dims, perm, es), pl) in enumerate(zip(problems, plans)):
+                b, nb = i % 2, problem_bytes((dims, perm, es))
+                with torch.cuda.stream(s_in):
+                    if done[b] is not None:
+                        s_in.wait_event(done[b])
+                    d_in[b][:nb].copy_(hin[:nb], non_blocking=True)
+                    loaded[b].record(s_in)
+                stream.wait_event(loaded[b])
+                if saved[b] is not None:
+                    stream.wait_event(saved[b])
+                pl.execute(d_in[b].data_ptr(), d_out[b].data_ptr())
+                done[b] = torch.cuda.Event()
+                done[b].record(stream)
+                with torch.cuda.stream(s_out):
+                    s_out.wait_event(done[b])
+                    hout[:nb].copy_(d_out[b][:nb], non_blocking=True)
+                    saved[b] = torch.cuda.Event()
+                    saved[b].record(s_out)
+            for ev in saved:
+                if ev is not None:
+                    stream.wait_event(ev)
 
         e2e_step()
         torch.cuda.synchronize(dev)
@@ -599,7 +631,10 @@ def run_grouped(args):
     peak, peak_kind = load_peaks()
 
     # end to end on a prefix of the batch whose inputs fit 2 GiB of pinned
-    # host memory: H2D of the inputs, the group, D2H of the outputs
+    # host memory.  The prefix is cut into E2E_CHUNKS contiguous groups of
+    # about equal bytes; chunk c + 1's input copy (own stream), group c
+    # (the plans' stream) and chunk c - 1's output copy (a third stream)
+    # overlap, the copies in opposite directions of the host link.
     e2e = None
     if not args.no_e2e:
         cap, m = 2 << 30, 0
@@ -609,27 +644,64 @@ def run_grouped(args):
         hin = torch.empty(sub_bytes, dtype=torch.uint8, pin_memory=True)
         hin.copy_(inp[:sub_bytes].cpu())
         hout = torch.empty(sub_bytes, dtype=torch.uint8, pin_memory=True)
-        with L.Group(plans[:m], ins[:m], outs[:m], stream, policy=policy) as sub:
-            def e2e_step():
-                inp[:sub_bytes].copy_(hin, non_blocking=True)
-                sub.execute()
-                hout.copy_(out[:sub_bytes], non_blocking=True)
+        cuts = [0]
+        for k in range(1, E2E_CHUNKS):
+            want = sub_bytes * k / E2E_CHUNKS
+            cuts.append(max(cuts[-1] + 1, next(i for i in range(m) if offs[i] >= want)))
+        cuts.append(m)
+        spans = []  # (first member, end member, first byte, end byte)
+        for a, b in zip(cuts, cuts[1:]):
+            spans.append((a, b, offs[a], offs[b - 1] + problem_bytes(problems[b - 1])))
+        groups = [L.Group(plans[a:b], ins[a:b], outs[a:b], stream, policy=policy)
+                  for a, b, _, _ in spans]
+        s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+        done = [None] * len(spans)   # group of the chunk finished (last step)
+        saved = [None] * len(spans)  # its outputs copied back (last step)
 
-            for _ in range(2):
-                e2e_step()
-            torch.cuda.synchronize(dev)
-            barrier(world)
-            e0.record(stream)
-            for _ in range(args.steps):
-                e2e_step()
-            e1.record(stream)
-            torch.cuda.synchronize(dev)
-            ems = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+        def e2e_step():
+            start = torch.cuda.Event()
+            start.record(stream)
+            s_in.wait_event(start)
+            s_out.wait_event(start)
+            for c, ((_, _, lo, hi), grp) in enumerate(zip(spans, groups)):
+                with torch.cuda.stream(s_in):
+                    if done[c] is not None:
+                        s_in.wait_event(done[c])
+                    inp[lo:hi].copy_(hin[lo:hi], non_blocking=True)
+                    loaded = torch.cuda.Event()
+                    loaded.record(s_in)
+                stream.wait_event(loaded)
+                if saved[c] is not None:
+                    stream.wait_event(saved[c])
+                grp.execute()
+                done[c] = torch.cuda.Event()
+                done[c].record(stream)
+                with torch.cuda.stream(s_out):
+                    s_out.wait_event(done[c])
+                    hout[lo:hi].copy_(out[lo:hi], non_blocking=True)
+                    saved[c] = torch.cuda.Event()
+                    saved[c].record(s_out)
+            for ev in saved:
+                stream.wait_event(ev)
+
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = max_over_ranks(e0.elapsed_time(e1), world) / args.steps
+        for grp in groups:
+            grp.destroy()
         e2e = {"value": round(world * m / (ems / 1e3), 1), "unit": "transposes/s",
                "h2d_bytes_per_step": sub_bytes, "d2h_bytes_per_step": sub_bytes,
-               "ms_per_step": round(ems, 3), "members": m,
+               "ms_per_step": round(ems, 3), "members": m, "chunks": len(spans),
                "note": f"first {m} problems of the batch (inputs within 2 GiB of pinned host "
-                       "memory), one H2D and one D2H copy of the packed buffers per step"}
+                       f"memory) in {len(spans)} groups; each step copies every input in and "
+                       "every output out, chunk copies overlapping the other chunks' groups"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
