@@ -1,0 +1,82 @@
+"""Parity at the benchmarks' full sizes, through the device verifier.
+
+The verifier (librett_c_verify, itself checked against the oracle with
+planted mistakes in test_gpu_verify.py) compares every output element with
+the input element the transpose formula names.  Here it checks
+* the whole 10,000-transpose grouped batch of the grouped benchmark
+  (30.3 GB in, 30.3 GB out), executed once as one group;
+* the first suite problems of the default benchmark at their full size
+  (1 GiB in, 1 GiB out each), planned by the default planner.
+"""
+import sys
+from pathlib import Path
+
+import pytest
+
+import librett_gb300 as L
+from librett_gb300.workloads import grouped_problems, packed_offsets
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _random_bytes(nbytes, seed):
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    words = (nbytes + 7) // 8
+    return torch.randint(-(2 ** 62), 2 ** 62, (words,), device="cuda", dtype=torch.int64,
+                         generator=g).view(torch.uint8)[:nbytes]
+
+
+def test_grouped_batch_every_member(cuda):
+    import torch
+
+    problems = grouped_problems(10000)
+    offs, total = packed_offsets(problems)
+    inp = _random_bytes(total, 11)
+    out = torch.zeros(total, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    base_in, base_out = inp.data_ptr(), out.data_ptr()
+    plans = [L.Plan(d, p, es, s) for d, p, es in problems]
+    try:
+        with L.Group(plans, [base_in + o for o in offs], [base_out + o for o in offs], s) as g:
+            g.execute()
+            torch.cuda.synchronize()
+        bad = []
+        for (d, p, es), o in zip(problems, offs):
+            n, first = L.verify(d, p, es, base_in + o, base_out + o, s)
+            if n:
+                bad.append((d, p, es, n, first))
+        assert not bad, bad[:5]
+    finally:
+        for pl in plans:
+            pl.destroy()
+    del inp, out
+    torch.cuda.empty_cache()
+
+
+def test_suite_problems_full_size(cuda):
+    import torch
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    problems = bench.suite_problems(200)[:12]
+    maxb = max(bench.problem_bytes(p) for p in problems)
+    inp = _random_bytes(maxb, 12)
+    out = torch.empty(maxb, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    methods = set()
+    for d, p, es in problems:
+        out.zero_()
+        with L.Plan(d, p, es, s) as pl:
+            methods.add(pl.info()["method"])
+            pl.execute(inp.data_ptr(), out.data_ptr())
+            n, first = L.verify(d, p, es, inp.data_ptr(), out.data_ptr(), s)
+        assert n == 0, (d, p, es, n, first)
+    assert len(methods) >= 3  # copies, tiles of several kinds
+    del inp, out
+    torch.cuda.empty_cache()
