@@ -156,7 +156,7 @@ def run_loop(out: Path, driver: Path, prefix: str, n: int, steps: int = 5, warmu
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--src", default="/root/reference/src")
-    ap.add_argument("--out", default=str(ROOT / "gpurun_out" / "ref"))
+    ap.add_argument("--out", default=str(ROOT / "oracle" / "_ref" / "results"))
     ap.add_argument("--engine", action="store_true",
                     help="also run every mode with the same driver linked to this engine")
     ap.add_argument("--engine-only", action="store_true",
