@@ -66,3 +66,18 @@ def test_grouped_distribution():
     assert all(sorted(p) == list(range(len(d))) for d, p, _ in probs)
     offs, total = packed_offsets(probs)
     assert all(o % 256 == 0 for o in offs) and total >= offs[-1] + vols[-1] * sizes[-1]
+
+
+def test_run_division_identity():
+    """The grouped kernel divides in-tile indices n < 2^16 by run lengths
+    d < 2^16 as umulhi(n + 1, floor((2^32 - 1) / d)) (RunDiv in plan.h).
+    Exhaustive over n for every d up to 4096 and 2,000 larger d, including
+    powers of two and the largest values."""
+    n = np.arange(1 << 16, dtype=np.uint64)
+    rng = np.random.default_rng(3)
+    ds = list(range(1, 4097)) + [1 << k for k in range(12, 16)] + [65535, 65534, 65533]
+    ds += rng.integers(4097, 65536, 2000).tolist()
+    for d in ds:
+        mul = np.uint64(0xFFFFFFFF // d)
+        q = ((n + np.uint64(1)) * mul) >> np.uint64(32)
+        assert np.array_equal(q, n // np.uint64(d)), d
