@@ -78,7 +78,7 @@ void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f) {
     computeStrides(f);
     return;
   }
-  int p1[MAXR];
+  int p1[MAXR] = {};  // r1 entries: perm is a bijection (checked by checkInput)
   int m = 0;
   for (int i = 0; i < rank; ++i)
     if (newIdx[perm[i]] >= 0) p1[m++] = newIdx[perm[i]];
