@@ -441,6 +441,14 @@ int librett_c_group_run_check(int rank, const int* dim, const int* permutation, 
   if (ldStep >= 0)
     for (size_t r = 0; r < ldRow.size(); ++r)
       if (ldRow[r] != (long long)r * ldStep) return LIBRETT_INTERNAL_ERROR;
+  const lt::GroupStoreSteps st = lt::groupStoreSteps(tp, rs, (int)sizeofType);
+  if (st.outStep >= 0)
+    for (size_t r = 0; r < stRow.size(); ++r)
+      if (stRow[r] != (long long)r * st.outStep || smRow[r] != (long long)r * st.rowSmStep)
+        return LIBRETT_INTERNAL_ERROR;
+  if (st.smStep >= 0)
+    for (size_t a = 0; a < smRun.size(); ++a)
+      if (smRun[a] != (long long)a * st.smStep) return LIBRETT_INTERNAL_ERROR;
   if (tp.tileVol >= 65536) return LIBRETT_INTERNAL_ERROR;  // run division needs indices < 2^16
   // the kernel's index arithmetic, unit by unit
   for (int u = 0; u < tp.nIn; ++u) {

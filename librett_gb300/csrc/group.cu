@@ -115,8 +115,10 @@ constexpr int STAGE_MAX = 8192;   // largest store-side table set staged in shar
 
 // Bytes of a member's store-side run tables (outRows, smRun) when they are
 // staged in shared memory, else 0.
-int stagedTableBytes(const TileParams& tp) {
+int stagedTableBytes(const TileParams& tp, int esize) {
   const GroupRunSplit rs = groupRunSplit(tp);
+  const GroupStoreSteps st = groupStoreSteps(tp, rs, esize);
+  if (st.outStep >= 0 && st.smStep >= 0) return 0;  // the kernel reads no store table
   size_t off[3];
   const size_t total = runTableBytes(tp, rs, off);
   const size_t bytes = total - off[1];
@@ -280,7 +282,7 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
   // the kernel's run division needs in-tile indices below 2^16 (RunDiv)
   if (out.tile.tileVol >= 65536) return false;
   // the tile data plus the staged store-side tables
-  out.smemBytes = out.tile.smStride * out.f.esize + stagedTableBytes(out.tile);
+  out.smemBytes = out.tile.smStride * out.f.esize + stagedTableBytes(out.tile, out.f.esize);
   return true;
 }
 
@@ -405,12 +407,16 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.inRun = makeRunDiv((uint32_t)rs.inRun);
       t.outRun = makeRunDiv((uint32_t)rs.outRun);
       t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
-      t.tabBytes = stagedTableBytes(tp);
+      t.tabBytes = stagedTableBytes(tp, m.pd.f.esize);
       t.smRunOff = (int)((sub[2] - sub[1]) / 4);
       t.padShift = tp.padShift;
       t.padLog = tp.padLog;
       const int step = groupLoadStep(tp, rs, m.pd.f.esize);
       t.ldStepBytes = step < 0 ? -1 : step * m.pd.f.esize;
+      const GroupStoreSteps st = groupStoreSteps(tp, rs, m.pd.f.esize);
+      t.outStepBytes = st.outStep < 0 ? -1 : st.outStep * m.pd.f.esize;
+      t.rowSmStep = st.rowSmStep;
+      t.smStep = st.smStep;
       GroupTableJob jb;
       std::memset(&jb, 0, sizeof(jb));
       jb.tp = tp;

@@ -48,6 +48,11 @@ struct GroupTensor {
   // input run r starts at r * ldStepBytes bytes from the tile corner when
   // >= 0 (evenly spaced runs; ldRow is then not read), else at ldRow[r]
   int ldStepBytes;
+  // evenly spaced store-side tables (outRows / smRun then not read):
+  // output run r at r * outStepBytes bytes and in-tile index r * rowSmStep
+  // when outStepBytes >= 0; run position a at in-tile index a * smStep when
+  // smStep >= 0
+  int outStepBytes, rowSmStep, smStep;
 };
 
 // One tile of a bucket, written on the device at group creation: the

@@ -284,6 +284,43 @@ int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize) {
   return (int)step;
 }
 
+GroupStoreSteps groupStoreSteps(const TileParams& tp, const GroupRunSplit& rs, int esize) {
+  GroupStoreSteps st;
+  long long so = 0, si = 0;
+  int prev = -1;
+  bool ok = true;
+  for (int i = rs.kOut; i < tp.nTR && ok; ++i) {
+    const int t = tp.trOut[i];
+    if (tp.trE[t] <= 1) continue;
+    if (prev < 0) {
+      so = tp.trSout[t];
+      si = tp.trInTile[t];
+    } else {
+      ok = (long long)tp.trSout[t] == (long long)tp.trE[prev] * tp.trSout[prev] &&
+           (long long)tp.trInTile[t] == (long long)tp.trE[prev] * tp.trInTile[prev];
+    }
+    prev = t;
+  }
+  if (ok && so * esize <= 0x7fffffffLL) {
+    st.outStep = (int)so;
+    st.rowSmStep = (int)si;
+  }
+  si = 0;
+  prev = -1;
+  ok = true;
+  for (int i = 0; i < rs.kOut && ok; ++i) {
+    const int t = tp.trOut[i];
+    if (tp.trE[t] <= 1) continue;
+    if (prev < 0)
+      si = tp.trInTile[t];
+    else
+      ok = (long long)tp.trInTile[t] == (long long)tp.trE[prev] * tp.trInTile[prev];
+    prev = t;
+  }
+  if (ok) st.smStep = (int)si;
+  return st;
+}
+
 void groupRunTablesHost(const TileParams& tp, const GroupRunSplit& rs, int* ldRow, int* stRow,
                         int* smRow, int* smRun) {
   for (int r = 0; r < tp.tileVol / rs.inRun; ++r) {

@@ -236,6 +236,17 @@ GroupRunSplit groupRunSplit(const TileParams& tp);
 // s * esize does not fit an int.
 int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize);
 
+// Steps of the store-side run tables where their entries are evenly spaced
+// (the same chain rule over the tile ranks in output order): output run r
+// starts r * outStep elements from the tile's output corner, at in-tile
+// index r * rowSmStep; position a of an output run holds in-tile index
+// a * smStep.  outStep = -1 (rows) or smStep = -1 (positions) where the
+// table is not evenly spaced, or outStep * esize does not fit an int.
+struct GroupStoreSteps {
+  int outStep = -1, rowSmStep = 0, smStep = -1;
+};
+GroupStoreSteps groupStoreSteps(const TileParams& tp, const GroupRunSplit& rs, int esize);
+
 // Host copy of the run tables: ldRow[tileVol / inRun] input offset of each
 // input run; stRow / smRow[tileVol / outRun] output offset and in-tile
 // (input-order) index of each output run's first element; smRun[outRun]

@@ -639,7 +639,12 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
   // nOut <= NL * TILE_THREADS * LV / SV
   constexpr int NS = (NL * LV + SV - 1) / SV;
   constexpr int UNROLL = NS <= 16 ? NS : 8;
-  auto storeAll = [&](const int2* outRows, const int* smRun) {
+  // ROWS: output runs evenly spaced (no outRows read); POS: positions of a
+  // run evenly spaced in the tile (no smRun read)
+  const int outStepB = g->outStepBytes, rowSmStep = g->rowSmStep, smStep = g->smStep;
+  auto storeAll = [&](auto rowsStepped, auto posStepped, const int2* outRows, const int* smRun) {
+    constexpr bool ROWS = decltype(rowsStepped)::value;
+    constexpr bool POS = decltype(posStepped)::value;
 #pragma unroll UNROLL
     for (int i = 0; i < NS; ++i) {
       if (i * TILE_THREADS < wMax) {
@@ -647,14 +652,28 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
         const uint32_t r = __umulhi((uint32_t)q1, outRun.mul);
         const int a1 = q1 - (int)r * outD;  // a + 1
         const int a = a1 - 1;
-        const int2 row = outRows[r];
-        ST* dst = reinterpret_cast<ST*>(offsetBytes(offsetBytes(outM1, a1, esR), row.x, esR));
-        const int jb = row.y;
+        ST* dst;
+        int jb;
+        if constexpr (ROWS) {
+          dst = reinterpret_cast<ST*>(offsetBytes(offsetBytes(outM1, a1, esR), (int)r, outStepB));
+          jb = (int)r * rowSmStep;
+        } else {
+          const int2 row = outRows[r];
+          dst = reinterpret_cast<ST*>(offsetBytes(offsetBytes(outM1, a1, esR), row.x, esR));
+          jb = row.y;
+        }
         if constexpr (SV == 1) {
-          *dst = ldShared<ES>(smAddr(jb + smRun[a]));
+          if constexpr (POS)
+            *dst = ldShared<ES>(smAddr(a * smStep + jb));
+          else
+            *dst = ldShared<ES>(smAddr(jb + smRun[a]));
         } else {
           T e[SV];
-          if constexpr (SV == 2) {
+          if constexpr (POS) {
+            const int x0 = a * smStep + jb;
+#pragma unroll
+            for (int c = 0; c < SV; ++c) e[c] = ldShared<ES>(smAddr(x0 + c * smStep));
+          } else if constexpr (SV == 2) {
             const int2 jr = *reinterpret_cast<const int2*>(smRun + a);
             e[0] = ldShared<ES>(smAddr(jb + jr.x));
             e[1] = ldShared<ES>(smAddr(jb + jr.y));
@@ -672,11 +691,28 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
       }
     }
   };
-  if (tabBytes > 0) {
-    const int* t = reinterpret_cast<const int*>(smraw);
-    storeAll(reinterpret_cast<const int2*>(smraw), t + g->smRunOff);
+  // tables that are read come from shared memory when staged, else from
+  // device memory (two instantiations, so shared reads stay shared loads)
+  auto withTables = [&](auto rowsStepped, auto posStepped) {
+    if (tabBytes > 0) {
+      const int* t = reinterpret_cast<const int*>(smraw);
+      storeAll(rowsStepped, posStepped, reinterpret_cast<const int2*>(smraw), t + g->smRunOff);
+    } else {
+      storeAll(rowsStepped, posStepped, g->outRows, g->smRun);
+    }
+  };
+  using Yes = std::true_type;
+  using No = std::false_type;
+  if (outStepB >= 0) {
+    if (smStep >= 0)
+      storeAll(Yes{}, Yes{}, nullptr, nullptr);
+    else
+      withTables(Yes{}, No{});
   } else {
-    storeAll(g->outRows, g->smRun);
+    if (smStep >= 0)
+      withTables(No{}, Yes{});
+    else
+      withTables(No{}, No{});
   }
 }
 
