@@ -50,7 +50,7 @@ std::unordered_map<int, DevInfo> gDevs;
 
 }  // namespace
 
-bool lt::currentDevice(int& dev, int& sms, std::string* name) {
+bool lt::currentDevice(int& dev, int& sms, const char** name) {
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   std::lock_guard<std::mutex> lk(gDevMu);
   auto it = gDevs.find(dev);
@@ -63,7 +63,15 @@ bool lt::currentDevice(int& dev, int& sms, std::string* name) {
     it = gDevs.emplace(dev, di).first;
   }
   sms = it->second.sms;
-  if (name) *name = it->second.name;
+  // entries are never erased and map nodes do not move: the name stays valid
+  if (name) *name = it->second.name.c_str();
+  return true;
+}
+
+bool lt::currentDevice(int& dev, int& sms, std::string* name) {
+  const char* n = nullptr;
+  if (!currentDevice(dev, sms, &n)) return false;
+  if (name) *name = n;
   return true;
 }
 
@@ -198,15 +206,20 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   if (handle == nullptr) return LIBRETT_INVALID_PARAMETER;
   if (lt::checkInput(rank, dim, perm, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
   int dev = 0, sms = 0;
-  std::string devName;
+  const char* devName = nullptr;
   if (!currentDevice(dev, sms, &devName)) return LIBRETT_INTERNAL_ERROR;
   lt::Fused f;
   lt::fuseRanks(rank, dim, perm, (int)sizeofType, f);
   std::string key;
+  bool cached = false;  // the cache is on (no key is built when it is off)
   if (candidate < 0) {
-    key = cacheKey(f, dev, sms);
-    std::unique_lock<std::mutex> lk(gCacheMu);
-    if (cacheCapacityLocked() > 0) {
+    {
+      std::lock_guard<std::mutex> lk(gCacheMu);
+      cached = cacheCapacityLocked() > 0;
+    }
+    if (cached) {
+      key = cacheKey(f, dev, sms);
+      std::unique_lock<std::mutex> lk(gCacheMu);
       auto it = gCache.find(key);
       if (it != gCache.end()) {
         gCacheLru.splice(gCacheLru.begin(), gCacheLru, it->second);
@@ -222,11 +235,11 @@ librettResult planImpl(librettHandle* handle, int rank, const int* dim, const in
   std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms, true);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   bool learned = false;
-  int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName.c_str(), &learned) : candidate;
+  int pick = candidate < 0 ? lt::choosePlan(cands, sms, devName, &learned) : candidate;
   if (pick >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
   if (!lt::refineCandidate(cands[pick], sms)) return LIBRETT_INTERNAL_ERROR;
   const int selectedBy = candidate >= 0 ? 3 : (learned ? 1 : 0);
-  if (candidate < 0) {
+  if (cached) {
     std::lock_guard<std::mutex> lk(gCacheMu);
     const int cap = cacheCapacityLocked();
     if (cap > 0 && gCache.find(key) == gCache.end()) {

@@ -515,7 +515,7 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide) {
 // the three pipelines.  Returns false when the tile does not fit the
 // kernels' limits.
 bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp,
-                       bool padSearch = true) {
+                       bool padSearch = true, long long noneWavefronts = -1) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
@@ -592,7 +592,10 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
     if (sh < tp.padLog || (!padSearch && sh != PAD_NONE)) continue;
-    long long w = wavefronts(tp, f.esize, sh, 64, jStore, nStore);
+    // the unpadded tile's count may be known from screening
+    long long w = sh == PAD_NONE && noneWavefronts >= 0
+                      ? noneWavefronts
+                      : wavefronts(tp, f.esize, sh, 64, jStore, nStore);
     if (best < 0 || w < best) {
       best = w;
       bestShift = sh;
@@ -937,7 +940,8 @@ bool refineCandidate(PlanDesc& pd, int numSMs) {
   if (pd.kernel != K_TILE || !pd.screened) return true;
   const int V = 16 / pd.f.esize;
   TileParams geom;
-  if (!buildTileGeometry(pd.f, pd.extent, V, V, geom, true)) return false;
+  // screening simulated the unpadded tile (the same geometry and units)
+  if (!buildTileGeometry(pd.f, pd.extent, V, V, geom, true, pd.tile.bankWavefronts)) return false;
   PlanDesc full;
   full.f = pd.f;
   full.targetRunBytes = pd.targetRunBytes;

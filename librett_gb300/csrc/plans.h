@@ -52,5 +52,6 @@ std::shared_ptr<PlanObj> findPlan(librettHandle h);
 
 // Current device, its SM count and (optionally) name, cached per device.
 bool currentDevice(int& dev, int& sms, std::string* name = nullptr);
+bool currentDevice(int& dev, int& sms, const char** name);
 
 }  // namespace lt

@@ -224,7 +224,12 @@ void denseRelu(const float* x, int n, int in, const float* wt, const float* b, f
 }  // namespace
 
 void mlpForwardBatch(const MlpModel& m, const float* x, int n, float* out) {
-  std::vector<float> a((size_t)n * MLP_HIDDEN), b((size_t)n * MLP_HIDDEN);
+  // activations of the layers, reused by the calling thread
+  thread_local std::vector<float> a, b;
+  if (a.size() < (size_t)n * MLP_HIDDEN) {
+    a.resize((size_t)n * MLP_HIDDEN);
+    b.resize((size_t)n * MLP_HIDDEN);
+  }
   const float* p = m.params.data();
   const float* b1 = p + MLP_HIDDEN * NFEAT;
   const float* b2 = b1 + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN;
