@@ -6,11 +6,14 @@ the input element the transpose formula names.  Here it checks
 * the whole 10,000-transpose grouped batch of the grouped benchmark
   (30.3 GB in, 30.3 GB out), executed once as one group;
 * the first suite problems of the default benchmark at their full size
-  (1 GiB in, 1 GiB out each), planned by the default planner.
+  (1 GiB in, 1 GiB out each), planned by the default planner;
+* volumes past 2^31 elements (LibreTT's 32-bit range; 8.6 and 17.2 GB each
+  way), with a round trip through the inverse permutation as well.
 """
 import sys
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 import librett_gb300 as L
@@ -79,4 +82,36 @@ def test_suite_problems_full_size(cuda):
         assert n == 0, (d, p, es, n, first)
     assert len(methods) >= 3  # copies, tiles of several kinds
     del inp, out
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("dims, perm, es", [
+    ([65539, 32769], [1, 0], 4),          # 2,147,647,491 elements, 8.6 GB each way
+    ([3, 46341, 15461], [2, 0, 1], 8),    # 2,149,434,603 elements, 17.2 GB each way
+])
+def test_beyond_2_31_elements(cuda, dims, perm, es):
+    """Volumes past 2^31 elements (LibreTT's int32 range): every output element
+    checked on the device, and the inverse permutation returns the input."""
+    import torch
+
+    vol = int(np.prod(dims))
+    assert vol > 2 ** 31
+    nbytes = vol * es
+    inp = _random_bytes(nbytes, 13)
+    out = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    with L.Plan(dims, perm, es, s) as p1:
+        p1.execute(inp.data_ptr(), out.data_ptr())
+        n, first = L.verify(dims, perm, es, inp.data_ptr(), out.data_ptr(), s)
+    assert n == 0, (n, first)
+    back = torch.empty_like(inp)
+    odims = [dims[p] for p in perm]
+    inv = [0] * len(perm)
+    for i, p in enumerate(perm):
+        inv[p] = i
+    with L.Plan(odims, inv, es, s) as p2:
+        p2.execute(out.data_ptr(), back.data_ptr())
+        torch.cuda.synchronize()
+    assert torch.equal(back, inp)
+    del inp, out, back
     torch.cuda.empty_cache()
