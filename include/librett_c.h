@@ -117,7 +117,7 @@ int librett_c_transpose_noalloc(int rank, const int* dim, const int* permutation
  * src/TensorTester.cpp:47-126): compares every element of odata with the
  * element of idata the transpose formula names, on the device, and returns
  * the number of mismatching elements and the smallest mismatching output
- * index (-1 if none).  Synchronises `stream`.  Fused dims must be < 2^31. */
+ * index (-1 if none).  Synchronises `stream`. */
 int librett_c_verify(int rank, const int* dim, const int* permutation, size_t sizeofType,
                      const void* idata, const void* odata, void* stream,
                      unsigned long long* mismatches, long long* first_bad);

@@ -17,8 +17,9 @@ namespace {
 struct VerifyParams {
   int rank;
   unsigned long long vol;
-  FastDiv outDim[MAXR];    // output-order dims (fused)
-  long long inStride[MAXR];  // input stride of output rank i (elements)
+  unsigned long long outD[MAXR];  // output-order dims (fused; may exceed 2^31)
+  FastDiv outDim[MAXR];           // their fast dividers (dims below 2^31)
+  long long inStride[MAXR];       // input stride of output rank i (elements)
 };
 
 // result[0]: mismatching elements; result[1]: smallest mismatching output index
@@ -34,9 +35,9 @@ verifyKernel(const __grid_constant__ VerifyParams p, const typename Word<ES>::T*
     unsigned long long rem = q;
     long long src = 0;
     for (int i = 0; i < p.rank; ++i) {
-      const unsigned long long d = p.outDim[i].d;
+      const unsigned long long d = p.outD[i];
       unsigned long long c;
-      if (rem < (1ull << 31)) {
+      if (rem < (1ull << 31) && d < (1ull << 31)) {
         const uint32_t qq = fdiv((uint32_t)rem, p.outDim[i]);
         c = rem - (unsigned long long)qq * d;
         rem = qq;
@@ -85,8 +86,8 @@ extern "C" int librett_c_verify(int rank, const int* dim, const int* permutation
   p.vol = (unsigned long long)f.vol;
   for (int i = 0; i < f.rank; ++i) {
     const int r = f.perm[i];
-    if (f.dim[r] >= (int64_t(1) << 31)) return LIBRETT_INVALID_PARAMETER;
-    p.outDim[i] = lt::makeFastDiv((uint32_t)f.dim[r]);
+    p.outD[i] = (unsigned long long)f.dim[r];
+    p.outDim[i] = lt::makeFastDiv(f.dim[r] < (int64_t(1) << 31) ? (uint32_t)f.dim[r] : 1u);
     p.inStride[i] = f.sin[r];
   }
   cudaStream_t s = (cudaStream_t)stream;

@@ -8,7 +8,8 @@ the input element the transpose formula names.  Here it checks
 * the first suite problems of the default benchmark at their full size
   (1 GiB in, 1 GiB out each), planned by the default planner;
 * volumes past 2^31 elements (LibreTT's 32-bit range; 8.6 and 17.2 GB each
-  way), with a round trip through the inverse permutation as well.
+  way) through the tile, copy and row-copy kernels, with a round trip through
+  the inverse permutation as well.
 """
 import sys
 from pathlib import Path
@@ -88,6 +89,8 @@ def test_suite_problems_full_size(cuda):
 @pytest.mark.parametrize("dims, perm, es", [
     ([65539, 32769], [1, 0], 4),          # 2,147,647,491 elements, 8.6 GB each way
     ([3, 46341, 15461], [2, 0, 1], 8),    # 2,149,434,603 elements, 17.2 GB each way
+    ([65539, 32769], [0, 1], 4),          # identity: one rank-1 copy
+    ([64, 33555, 1001], [0, 2, 1], 4),    # leading rank kept: 2,149,667,520 elements
 ])
 def test_beyond_2_31_elements(cuda, dims, perm, es):
     """Volumes past 2^31 elements (LibreTT's int32 range): every output element
@@ -114,4 +117,23 @@ def test_beyond_2_31_elements(cuda, dims, perm, es):
         torch.cuda.synchronize()
     assert torch.equal(back, inp)
     del inp, out, back
+    torch.cuda.empty_cache()
+
+
+def test_row_copy_beyond_2_31_elements(cuda):
+    """The row-copy kernel (LibreTT's TiledCopy) past 2^31 elements: its
+    candidate is the first one whenever the leading rank stays in place."""
+    import torch
+
+    dims, perm, es = [64, 33555, 1001], [0, 2, 1], 4
+    vol = int(np.prod(dims))
+    inp = _random_bytes(vol * es, 14)
+    out = torch.empty(vol * es, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    with L.Plan(dims, perm, es, s, candidate=0) as p:
+        assert L.METHOD_NAMES[p.info()["method"]] == "TiledCopy"
+        p.execute(inp.data_ptr(), out.data_ptr())
+        n, first = L.verify(dims, perm, es, inp.data_ptr(), out.data_ptr(), s)
+    assert n == 0, (n, first)
+    del inp, out
     torch.cuda.empty_cache()
