@@ -137,12 +137,20 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        rows = []
-        for line in Path(self.path).read_text().splitlines():
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
-                rows.append(parts)
+        text = Path(self.path).read_text()
         os.unlink(self.path)
+        after = False
+        if not self._rows(text):
+            # a region shorter than the sampling period: one reading right after it
+            try:
+                text = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                    timeout=30).stdout
+                after = True
+            except (OSError, subprocess.TimeoutExpired):
+                return None
+        rows = self._rows(text)
         if not rows:
             return None
         sm = [float(r[1]) for r in rows]
@@ -154,8 +162,20 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         loaded = [x for x in sm if x > 0.5 * smax] or sm
-        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(rows)}
+        out = {"sm_mhz": statistics.median(loaded), "sm_max_mhz": smax,
+               "reasons": sorted(reasons), "samples": 0 if after else len(rows)}
+        if after:
+            out["note"] = "timed region shorter than the 100 ms sampling period: one reading after it"
+        return out
+
+    @staticmethod
+    def _rows(text):
+        rows = []
+        for line in text.splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                rows.append(parts)
+        return rows
 
 
 def dist_setup(n_gpus):
