@@ -100,7 +100,11 @@ librettResult librettExecute(librettHandle handle, void* idata, void* odata);
  * destruction frees in stream order.  The member plans may be destroyed once
  * the group exists (the group keeps what it needs).  Every member runs as a
  * flat tile inside its bucket (in element units when its pointers are not
- * 16-byte aligned). */
+ * 16-byte aligned).  Members run concurrently, so their buffers must be
+ * independent: no member's output may overlap any member's input or output
+ * (inputs may overlap each other).  A batch where one member reads what
+ * another writes must use librettExecute in order instead; creation checks
+ * the byte ranges and returns LIBRETT_INVALID_PARAMETER on an overlap. */
 typedef unsigned int librettGroupHandle;
 
 librettResult librettGroupCreate(librettGroupHandle* group, int count, const librettHandle* plans,

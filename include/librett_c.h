@@ -188,16 +188,14 @@ int librett_c_group_create(librettGroupHandle* group, int count, const librettHa
  * tile + 4 * loads: tile 0 = plan selector's tile, 1 = largest tile within
  * 10% of the best sector efficiency, 2 = largest tile, 3 = analytic model for
  * a full device; loads 0 = through registers, 1 = cp.async into shared
- * memory, 2 = aligned 16-byte reads of each input run scattered into shared
- * memory (element-size load units narrower than 16 bytes; others use 1).
- * Values 0..11. */
+ * memory.  Values 0..7. */
 int librett_c_group_create_policy(librettGroupHandle* group, int count,
                                   const librettHandle* plans, void* const* idata,
                                   void* const* odata, void* stream, const int* policy);
 int librett_c_group_tune(librettGroupHandle group);
 /* Bucket `index` (launch order) of the group's graph: shape[6] = element
  * bytes, load unit, store unit (elements), load units per thread, dynamic
- * shared memory bytes, loads (0/1/2 as in the policy); its members, tiles
+ * shared memory bytes, loads (0/1 as in the policy); its members, tiles
  * and algorithmic bytes. */
 int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int* members,
                            long long* tiles, long long* bytes);
@@ -231,6 +229,24 @@ int librett_c_group_info(librettGroupHandle group, int* members, int* buckets, i
 /* Number of device kernel launches this library issued since load (all
  * threads, all devices).  Used to count launches inside a timed region. */
 unsigned long long librett_c_launch_count(void);
+
+/* Device memory the plan-table arena has requested since load (all
+ * devices): bytes of 8 MiB slabs from cudaMalloc, table blocks handed out,
+ * and bytes of large tables from its stream-ordered pool.  No LibreTT
+ * counterpart (LibreTT calls cudaMalloc per plan, src/plan.cpp:1648-1676). */
+int librett_c_table_arena_stats(long long* slab_bytes, long long* blocks, long long* pool_bytes);
+
+/* Host-side fault injection, for tests of the error paths.  LibreTT exits
+ * the process on a CUDA error (src/GpuUtils.h:47-56); this library returns
+ * LIBRETT_INTERNAL_ERROR and stays usable.  Arms `site` so that, after
+ * `after` more calls at that site succeed, the next one reports a CUDA error
+ * on the host without calling the device, then disarms (after < 0 disarms
+ * at once).  Sites: 0 plan-table allocation (librettPlan,
+ * librettPlanMeasure), 1 a group's device image (librettGroupCreate),
+ * 2 any transpose launch (librettExecute, group execution, the
+ * no-allocation transpose).  Returns LIBRETT_INVALID_PARAMETER for another
+ * site. */
+int librett_c_inject_fault(int site, long long after);
 
 /* Human-readable name of a result code. */
 const char* librett_c_result_string(int result);

@@ -264,6 +264,26 @@ def launch_count() -> int:
     return int(_lib.load().librett_c_launch_count())
 
 
+def table_arena_stats() -> dict:
+    """Device memory the plan-table arena requested since load: slab bytes
+    (cudaMalloc), table blocks handed out, bytes from its pool."""
+    v = [ctypes.c_longlong(0) for _ in range(3)]
+    _lib.load().librett_c_table_arena_stats(*[ctypes.byref(x) for x in v])
+    return {"slab_bytes": v[0].value, "blocks": v[1].value, "pool_bytes": v[2].value}
+
+
+FAULT_TABLE_ALLOC, FAULT_GROUP_ALLOC, FAULT_LAUNCH = 0, 1, 2
+
+
+def inject_fault(site: int, after: int = 0) -> None:
+    """Arm a host-side failure at `site` (FAULT_*): after `after` more calls
+    there succeed, the next one reports a CUDA error without reaching the
+    device; after < 0 disarms."""
+    rc = _lib.load().librett_c_inject_fault(int(site), int(after))
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_inject_fault")
+
+
 class Plan:
     """Owning wrapper of a plan handle."""
 

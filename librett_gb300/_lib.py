@@ -143,6 +143,10 @@ C_FUNCTIONS = [
       ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_longlong),
       ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_launch_count", ctypes.c_ulonglong, []),
+    ("librett_c_table_arena_stats", ctypes.c_int,
+     [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+      ctypes.POINTER(ctypes.c_longlong)]),
+    ("librett_c_inject_fault", ctypes.c_int, [ctypes.c_int, ctypes.c_longlong]),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]
 

@@ -18,6 +18,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fault.h"
 #include "launch.h"
 #include "librett.h"
 #include "librett_c.h"
@@ -565,3 +566,12 @@ const char* librett_c_result_string(int result) {
 }
 
 }  // extern "C"
+
+int librett_c_inject_fault(int site, long long after) {
+  return lt::armFault(site, after) ? LIBRETT_SUCCESS : LIBRETT_INVALID_PARAMETER;
+}
+
+int librett_c_table_arena_stats(long long* slab_bytes, long long* blocks, long long* pool_bytes) {
+  lt::tableArenaStats(slab_bytes, blocks, pool_bytes);
+  return LIBRETT_SUCCESS;
+}

@@ -15,6 +15,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fault.h"
 #include "group.h"
 #include "kernels.cuh"
 #include "launch.h"
@@ -100,15 +101,14 @@ size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[3
 
 // Policies: policy % GP_TILES picks a member's flat tile from its
 // candidates; policy / GP_TILES picks the bucket's loads (0 registers,
-// 1 cp.async, 2 aligned 16-byte run reads where the load units are narrower
-// than 16 bytes, else cp.async).
+// 1 cp.async).
 enum GroupPolicy {
   GP_SELECTOR = 0,  // the plan selector's choice for the tensor on its own
   GP_WIDE = 1,      // the largest tile within 10% of the best sector efficiency
   GP_WIDEST = 2,    // the largest tile
   GP_FILL = 3,      // the analytic model with the device assumed full of other work
   GP_TILES = 4,
-  GP_COUNT = 3 * GP_TILES
+  GP_COUNT = 2 * GP_TILES
 };
 constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
 constexpr int STAGE_MAX = 8192;   // largest store-side table set staged in shared memory
@@ -321,8 +321,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       continue;
     }
     const PlanDesc& pd = m.pd;
-    int loads = pol[m.cls] / GP_TILES;
-    if (loads == 2 && (pd.tile.lv > 1 || pd.f.esize == 16)) loads = 1;  // run reads need narrow units
+    const int loads = pol[m.cls] / GP_TILES;
     auto key = std::make_tuple(pd.f.esize, pd.tile.lv, pd.tile.sv, pd.slots, loads,
                                (pd.smemBytes + SMEM_CLASS - 1) / SMEM_CLASS);
     auto it = key2b.find(key);
@@ -376,7 +375,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
       off = align16(off + runTableBytes(tp, groupRunSplit(tp), sub));
     }
   const size_t total = std::max<size_t>(off, 16);
-  if (cudaMallocAsync(&B.alloc, total, g.stream) != cudaSuccess) {
+  if (injectFault(FAULT_GROUP_ALLOC) || cudaMallocAsync(&B.alloc, total, g.stream) != cudaSuccess) {
     B.alloc = nullptr;
     return LIBRETT_INTERNAL_ERROR;
   }
@@ -406,7 +405,6 @@ librettResult build(GroupObj& g, const Policy& pol) {
       t.nOut = tp.nOut;
       t.inRun = makeRunDiv((uint32_t)rs.inRun);
       t.outRun = makeRunDiv((uint32_t)rs.outRun);
-      t.inSlots = makeFastDiv((uint32_t)((rs.inRun * m.pd.f.esize + 15 - m.pd.f.esize) / 16 + 1));
       t.tabBytes = stagedTableBytes(tp, m.pd.f.esize);
       t.smRunOff = (int)((sub[2] - sub[1]) / 4);
       t.padShift = tp.padShift;
@@ -524,6 +522,33 @@ uint64_t batchSignature(const GroupObj& g) {
   return h;
 }
 
+// Members run concurrently (one bucket launch holds many; buckets run on
+// parallel graph branches), so no member's output may overlap any member's
+// input or output.  Sweep over the byte ranges sorted by start: a range
+// overlaps an earlier one iff the largest end seen so far exceeds its
+// start; inputs may overlap inputs.
+bool independentBuffers(const GroupObj& g) {
+  struct Range {
+    uintptr_t lo, hi;
+    bool out;
+  };
+  std::vector<Range> r;
+  r.reserve(2 * g.members.size());
+  for (const Member& m : g.members) {
+    const uintptr_t n = (uintptr_t)(m.plan->pd.f.vol * m.plan->pd.f.esize);
+    r.push_back({(uintptr_t)m.in, (uintptr_t)m.in + n, false});
+    r.push_back({(uintptr_t)m.out, (uintptr_t)m.out + n, true});
+  }
+  std::sort(r.begin(), r.end(), [](const Range& a, const Range& b) { return a.lo < b.lo; });
+  uintptr_t endAny = 0, endOut = 0;
+  for (const Range& x : r) {
+    if (x.out ? endAny > x.lo : endOut > x.lo) return false;
+    endAny = std::max(endAny, x.hi);
+    if (x.out) endOut = std::max(endOut, x.hi);
+  }
+  return true;
+}
+
 librettResult create(librettGroupHandle* handle, int count, const librettHandle* plans,
                      void* const* idata, void* const* odata, cudaStream_t stream,
                      const int* policy) {
@@ -556,6 +581,7 @@ librettResult create(librettGroupHandle* handle, int count, const librettHandle*
     m.cls = memberClass(bytes, f.esize);
     m.aligned16 = (uintptr_t)m.in % 16 == 0 && (uintptr_t)m.out % 16 == 0;
   }
+  if (!independentBuffers(*g)) return LIBRETT_INVALID_PARAMETER;
   g->signature = batchSignature(*g);
   // Untuned default: the largest tiles, loaded by cp.async (the fastest
   // uniform policy on the 10,000-tensor batch of rank 2..6, 2^10..2^22
@@ -590,7 +616,8 @@ std::shared_ptr<GroupObj> findGroup(librettGroupHandle h) {
 }
 
 librettResult launch(GroupObj& g) {
-  if (g.built.exec == nullptr || cudaGraphLaunch(g.built.exec, g.stream) != cudaSuccess)
+  if (g.built.exec == nullptr || injectFault(FAULT_LAUNCH) ||
+      cudaGraphLaunch(g.built.exec, g.stream) != cudaSuccess)
     return LIBRETT_INTERNAL_ERROR;
   gLaunchCount.fetch_add((unsigned long long)g.built.buckets + g.built.separate,
                          std::memory_order_relaxed);

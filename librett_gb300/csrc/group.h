@@ -40,7 +40,6 @@ struct GroupTensor {
   const int* smRun;  // [outRun] in-tile index of each element of an output run, from the first
   int nIn, nOut;       // load / store units of a tile
   RunDiv inRun, outRun;  // run lengths (in-tile indices are < 2^16)
-  FastDiv inSlots;  // aligned 16-byte blocks reserved per input run (loads 2)
   // Store-side tables staged in shared memory: their bytes (0 = read from
   // device memory) and the int offset of smRun inside them (outRows first).
   int tabBytes, smRunOff;

@@ -7,11 +7,38 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fault.h"
 #include "kernels.cuh"
 
 namespace lt {
 
 std::atomic<unsigned long long> gLaunchCount{0};
+
+namespace {
+std::atomic<long long> gFaultAfter[FAULT_SITES] = {{-1}, {-1}, {-1}};
+std::atomic<long long> gArenaSlabBytes{0}, gArenaBlocks{0}, gArenaPoolBytes{0};
+}  // namespace
+
+bool injectFault(int site) {
+  std::atomic<long long>& a = gFaultAfter[site];
+  long long v = a.load(std::memory_order_relaxed);
+  while (v >= 0) {
+    if (a.compare_exchange_weak(v, v - 1, std::memory_order_relaxed)) return v == 0;
+  }
+  return false;
+}
+
+bool armFault(int site, long long after) {
+  if (site < 0 || site >= FAULT_SITES) return false;
+  gFaultAfter[site].store(after < 0 ? -1 : after, std::memory_order_relaxed);
+  return true;
+}
+
+void tableArenaStats(long long* slabBytes, long long* blocks, long long* poolBytes) {
+  if (slabBytes) *slabBytes = gArenaSlabBytes.load();
+  if (blocks) *blocks = gArenaBlocks.load();
+  if (poolBytes) *poolBytes = gArenaPoolBytes.load();
+}
 
 int cachedOccupancy(const void* func, int threads, int smem) {
   static std::mutex mu;
@@ -240,6 +267,8 @@ TableArena& tableArena() {
 
 cudaError_t tableAlloc(size_t bytes, cudaStream_t s, void** out) {
   *out = nullptr;
+  if (injectFault(FAULT_TABLE_ALLOC)) return cudaErrorMemoryAllocation;
+  gArenaBlocks.fetch_add(1, std::memory_order_relaxed);
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
   if (err != cudaSuccess) return err;
@@ -251,6 +280,7 @@ cudaError_t tableAlloc(size_t bytes, cudaStream_t s, void** out) {
     err = tablePool(&pool);
     if (err == cudaSuccess) err = cudaMallocFromPoolAsync(out, bytes, pool, s);
     if (err != cudaSuccess) return err;
+    gArenaPoolBytes.fetch_add((long long)bytes, std::memory_order_relaxed);
     TableBlock* b = new TableBlock();
     b->p = *out;
     b->device = dev;
@@ -306,6 +336,7 @@ cudaError_t tableAlloc(size_t bytes, cudaStream_t s, void** out) {
     void* slab = nullptr;
     err = cudaMalloc(&slab, TABLE_SLAB);
     if (err != cudaSuccess) return err;
+    gArenaSlabBytes.fetch_add((long long)TABLE_SLAB, std::memory_order_relaxed);
     std::lock_guard<std::mutex> lk(A.mu);
     TableArena::Dev& D = A.devs[dev];
     D.cur = static_cast<char*>(slab);
@@ -367,6 +398,7 @@ void destroyDeviceTables(void* alloc, cudaStream_t s) { tableFree(alloc, s); }
 
 cudaError_t launchPlan(const PlanDesc& pd, const DeviceTables* dt, const void* in, void* out,
                        cudaStream_t s, int numSMs, int* grid) {
+  if (injectFault(FAULT_LAUNCH)) return cudaErrorLaunchFailure;
   const uintptr_t align = (uintptr_t)in | (uintptr_t)out;
   int g = 0;
   cudaError_t err = cudaErrorInvalidValue;

@@ -26,6 +26,7 @@
 #include "librett.h"
 #include "librett_c.h"
 #include "plan.h"
+#include "plans.h"
 #include "select.h"
 
 namespace lt {
@@ -38,33 +39,27 @@ constexpr size_t kScratchBytes = 64 * 1024;
 
 __device__ __align__(256) unsigned char gTableScratch[kScratchBytes];
 
-struct DeviceScratch {
-  unsigned char* ptr = nullptr;
-  int numSMs = 0;
-};
-
 std::mutex gScratchMu;
-std::unordered_map<int, DeviceScratch> gScratch;
+std::unordered_map<int, unsigned char*> gScratch;
 
 // Per-device set-up, done by the first call with that device current:
 // resolve the array's device address (the host-side symbol is only a
-// stand-in) and the SM count.
-cudaError_t scratchFor(int dev, DeviceScratch& out) {
+// stand-in).  The address is kept for the life of the process, keyed by
+// device ordinal; after a cudaDeviceReset of a device already used here it
+// is stale, so this entry point (like the library's plan-table arena) is
+// not supported across a device reset.
+cudaError_t scratchFor(int dev, unsigned char** out) {
   std::lock_guard<std::mutex> lk(gScratchMu);
   auto it = gScratch.find(dev);
   if (it != gScratch.end()) {
-    out = it->second;
+    *out = it->second;
     return cudaSuccess;
   }
-  DeviceScratch ds;
   void* p = nullptr;
   cudaError_t err = cudaGetSymbolAddress(&p, gTableScratch);
   if (err != cudaSuccess) return err;
-  err = cudaDeviceGetAttribute(&ds.numSMs, cudaDevAttrMultiProcessorCount, dev);
-  if (err != cudaSuccess) return err;
-  ds.ptr = static_cast<unsigned char*>(p);
-  gScratch[dev] = ds;
-  out = ds;
+  gScratch[dev] = static_cast<unsigned char*>(p);
+  *out = static_cast<unsigned char*>(p);
   return cudaSuccess;
 }
 
@@ -79,17 +74,20 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   if (idata == nullptr || odata == nullptr || idata == odata) return LIBRETT_INVALID_PARAMETER;
   const size_t a = sizeofType < 16 ? sizeofType : 16;
   if ((uintptr_t)idata % a != 0 || (uintptr_t)odata % a != 0) return LIBRETT_INVALID_PARAMETER;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
-  DeviceScratch ds;
-  if (scratchFor(dev, ds) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  // the device, its SM count and name as librettPlan sees them, so both
+  // paths rank candidates with the same (device-keyed) selector
+  int dev = 0, sms = 0;
+  const char* devName = nullptr;
+  if (!currentDevice(dev, sms, &devName)) return LIBRETT_INTERNAL_ERROR;
+  unsigned char* scratch = nullptr;
+  if (scratchFor(dev, &scratch) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   cudaStream_t s = (cudaStream_t)stream;
 
   Fused f;
   fuseRanks(rank, dim, permutation, (int)sizeofType, f);
-  std::vector<PlanDesc> cands = enumerateCandidates(f, ds.numSMs, true);
+  std::vector<PlanDesc> cands = enumerateCandidates(f, sms, true);
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
-  int pick = choosePlan(cands, ds.numSMs, nullptr, nullptr);
+  int pick = choosePlan(cands, sms, devName, nullptr);
   // Tile problems run the flat pipeline, whose tables go to the scratch.
   if (cands[pick].kernel == K_TILE && cands[pick].pipe != PIPE_FLAT) {
     int flat = -1;
@@ -99,7 +97,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
         flat = (int)c;
     if (flat >= 0) pick = flat;
   }
-  if (!refineCandidate(cands[pick], ds.numSMs) || !finalizePlan(cands[pick]))
+  if (!refineCandidate(cands[pick], sms) || !finalizePlan(cands[pick]))
     return LIBRETT_INTERNAL_ERROR;
   const PlanDesc& pd = cands[pick];
   DeviceTables dt;
@@ -109,10 +107,10 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
     size_t stOffset, smOffset;
     if (deviceTableBytes(pd.tile, &stOffset, &smOffset) > kScratchBytes)
       return LIBRETT_INVALID_PARAMETER;  // tables exceed the scratch
-    if (writeDeviceTables(pd.tile, ds.ptr, s, &dt) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+    if (writeDeviceTables(pd.tile, scratch, s, &dt) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
   }
   int grid = 0;
-  if (launchPlan(pd, &dt, idata, odata, s, ds.numSMs, &grid) != cudaSuccess)
+  if (launchPlan(pd, &dt, idata, odata, s, sms, &grid) != cudaSuccess)
     return LIBRETT_INTERNAL_ERROR;
   return LIBRETT_SUCCESS;
 }

@@ -503,14 +503,9 @@ __device__ __forceinline__ void stShared(uint32_t addr, const typename Word<BYTE
 // run plus the position inside the run, so the tables stay in L1 even when
 // consecutive CTAs belong to different tensors; when they are small enough
 // the store-side tables are copied into shared memory with the data.  LOADS:
-// 0 stages the load
-// units in registers; 1 copies them with cp.async straight into shared
-// memory (no data registers, so more CTAs fit an SM); 2, for element-size
-// load units narrower than 16 bytes, reads each input run with aligned
-// 16-byte loads and scatters the run's elements into shared memory.  An
-// aligned 16-byte block that holds a byte of the tensor lies in the same
-// memory page as that byte, so these reads stay in mapped memory even where
-// the block extends past the tensor; the bytes outside the run are dropped.
+// 0 stages the load units in registers; 1 copies them with cp.async straight
+// into shared memory (no data registers, so more CTAs fit an SM).  Every
+// access stays inside the member's input and output tensors.
 //
 // Index arithmetic is kept off the ALU pipe where it can be: with element-
 // size units the kernel does little else, and integer adds, shifts and
@@ -541,32 +536,7 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
   const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
   const int esR = opaque(ES);
   const int padMul = 1 << padLog;
-  auto pad = [&](int j) { return j + ((j >> padShift) << padLog); };
-  if constexpr (LOADS == 2 && LV == 1 && ES < 16) {
-    constexpr int CH = 16 / ES;  // elements per 16-byte block
-    const int R = (int)inRun.d;
-    const FastDiv slots = g->inSlots;  // blocks reserved per run
-    const int items = (nIn / R) * (int)slots.d;
-#pragma unroll 4
-    for (int w = threadIdx.x; w < items; w += TILE_THREADS) {
-      const uint32_t r = fdiv((uint32_t)w, slots);
-      const int c = w - (int)(r * slots.d);
-      const long long A = (long long)reinterpret_cast<uintptr_t>(in + __ldg(ldRow + r));
-      const long long blk = (A & ~15LL) + 16LL * c;
-      if (blk < A + (long long)R * ES) {
-        const uint4 val = __ldg(reinterpret_cast<const uint4*>(blk));
-        T e[CH];
-        __builtin_memcpy(e, &val, sizeof(val));
-        const int a0 = (int)((blk - A) / ES);
-        const int j0 = (int)r * R;
-#pragma unroll
-        for (int k = 0; k < CH; ++k) {
-          const int a = a0 + k;
-          if (a >= 0 && a < R) s[pad(j0 + a)] = e[k];
-        }
-      }
-    }
-  } else {
+  {
     constexpr int B = TILE_THREADS * LV;
     const int jT = threadIdx.x * LV;
     const int bR = opaque(B);

@@ -1,0 +1,137 @@
+"""CUDA-error paths, driven by host-side fault injection.
+
+LibreTT exits the process on any CUDA error (src/GpuUtils.h:47-56).  This
+library returns LIBRETT_INTERNAL_ERROR instead and must stay usable.  The
+failures here are made on the host (librett_c_inject_fault reports a CUDA
+error before the device is called), so no GPU ever faults: each test arms one
+site, checks the error code, then checks that the next call through the same
+path succeeds and transposes correctly.
+"""
+import numpy as np
+import pytest
+
+import librett_gb300 as L
+from librett_gb300 import _lib
+from oracle import oracle as O
+
+DIMS, PERM, ES = [37, 8, 19, 6], [2, 0, 3, 1], 8  # a tile plan with device tables
+
+
+def _data(dims, es, seed=3):
+    import torch
+
+    host = np.random.default_rng(seed).integers(0, 256, int(np.prod(dims)) * es, dtype=np.uint8)
+    return host, torch.from_numpy(host).cuda()
+
+
+@pytest.fixture
+def disarm():
+    yield
+    for site in (L.FAULT_TABLE_ALLOC, L.FAULT_GROUP_ALLOC, L.FAULT_LAUNCH):
+        L.inject_fault(site, -1)
+
+
+def test_fault_sites_are_validated():
+    lib = _lib.load()
+    assert lib.librett_c_inject_fault(3, 0) == L.LIBRETT_INVALID_PARAMETER
+    assert lib.librett_c_inject_fault(-1, 0) == L.LIBRETT_INVALID_PARAMETER
+    for site in (0, 1, 2):
+        assert lib.librett_c_inject_fault(site, -1) == L.LIBRETT_SUCCESS
+
+
+@pytest.mark.gpu
+def test_plan_table_allocation_failure(cuda, disarm):
+    import torch
+
+    host, inp = _data(DIMS, ES)
+    out = torch.zeros_like(inp)
+    s = torch.cuda.current_stream()
+    lib = _lib.load()
+    prev = lib.librett_c_set_plan_cache(0)
+    try:
+        L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
+        with pytest.raises(L.LibrettError) as e:
+            L.Plan(DIMS, PERM, ES, s)
+        assert e.value.code == L.LIBRETT_INTERNAL_ERROR
+        L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
+        with pytest.raises(L.LibrettError) as e:
+            L.Plan(DIMS, PERM, ES, s, measure=(inp.data_ptr(), out.data_ptr()))
+        assert e.value.code == L.LIBRETT_INTERNAL_ERROR
+        # disarmed after firing: the same calls now succeed
+        with L.Plan(DIMS, PERM, ES, s) as p:
+            assert L.METHOD_NAMES[p.info()["method"]] != "Trivial"
+            p.execute(inp.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        assert np.array_equal(out.cpu().numpy(), O.transpose_np(host, DIMS, PERM, ES).view(np.uint8))
+    finally:
+        lib.librett_c_set_plan_cache(prev)
+
+
+@pytest.mark.gpu
+def test_execute_launch_failure(cuda, disarm):
+    import torch
+
+    host, inp = _data(DIMS, ES)
+    out = torch.zeros_like(inp)
+    s = torch.cuda.current_stream()
+    want = O.transpose_np(host, DIMS, PERM, ES).view(np.uint8)
+    with L.Plan(DIMS, PERM, ES, s) as p:
+        L.inject_fault(L.FAULT_LAUNCH, 1)  # the first execute passes, the second fails
+        p.execute(inp.data_ptr(), out.data_ptr())
+        with pytest.raises(L.LibrettError) as e:
+            p.execute(inp.data_ptr(), out.data_ptr())
+        assert e.value.code == L.LIBRETT_INTERNAL_ERROR
+        out.zero_()
+        p.execute(inp.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), want)
+
+
+@pytest.mark.gpu
+def test_group_failures(cuda, disarm):
+    import torch
+
+    probs = [(DIMS, PERM, ES), ([33, 17], [1, 0], 4), ([5, 7, 9, 3], [3, 1, 0, 2], 16)]
+    nbytes = [int(np.prod(d)) * e for d, _, e in probs]
+    offs = np.concatenate([[0], np.cumsum([(n + 255) // 256 * 256 for n in nbytes])])
+    host = np.random.default_rng(5).integers(0, 256, int(offs[-1]), dtype=np.uint8)
+    gin = torch.from_numpy(host).cuda()
+    gout = torch.zeros_like(gin)
+    s = torch.cuda.current_stream()
+    ins = [gin.data_ptr() + int(o) for o in offs[:-1]]
+    outs = [gout.data_ptr() + int(o) for o in offs[:-1]]
+    plans = [L.Plan(d, p, e, s) for d, p, e in probs]
+    try:
+        L.inject_fault(L.FAULT_GROUP_ALLOC, 0)
+        with pytest.raises(L.LibrettError) as e:
+            L.Group(plans, ins, outs, s)
+        assert e.value.code == L.LIBRETT_INTERNAL_ERROR
+        with L.Group(plans, ins, outs, s) as g:
+            L.inject_fault(L.FAULT_LAUNCH, 0)
+            with pytest.raises(L.LibrettError) as e:
+                g.execute()
+            assert e.value.code == L.LIBRETT_INTERNAL_ERROR
+            g.execute()
+            torch.cuda.synchronize()
+        res = gout.cpu().numpy()
+        for (d, p, e), o, n in zip(probs, offs, nbytes):
+            assert np.array_equal(res[o:o + n], O.transpose_np(host[o:o + n], d, p, e).view(np.uint8))
+    finally:
+        for p in plans:
+            p.destroy()
+
+
+@pytest.mark.gpu
+def test_noalloc_launch_failure(cuda, disarm):
+    import torch
+
+    host, inp = _data(DIMS, ES)
+    out = torch.zeros_like(inp)
+    s = torch.cuda.current_stream()
+    L.inject_fault(L.FAULT_LAUNCH, 0)
+    assert L.transpose_noalloc(DIMS, PERM, ES, s, inp.data_ptr(),
+                               out.data_ptr()) == L.LIBRETT_INTERNAL_ERROR
+    assert L.transpose_noalloc(DIMS, PERM, ES, s, inp.data_ptr(),
+                               out.data_ptr()) == L.LIBRETT_SUCCESS
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), O.transpose_np(host, DIMS, PERM, ES).view(np.uint8))

@@ -6,8 +6,11 @@ allocator, or allocation forbidden on a latency-critical path).  It keeps
 the flat tile kernel's offset tables in one fixed device array instead of a
 per-plan allocation.  Here its outputs must equal, bit for bit, the outputs
 of librettPlan + librettExecute on the same inputs, on two calls in a row
-(the second call reuses the array the first one wrote).  The file sorts
-last so that a run stopping at the first failure has run everything else.
+(the second call reuses the array the first one wrote), with pointers
+aligned to 16 bytes and with pointers aligned only to the element; and the
+calls must leave the library's device-memory counters and the device's free
+memory unchanged.  The file sorts last so that a run stopping at the first
+failure has run everything else.
 """
 import numpy as np
 import pytest
@@ -44,12 +47,63 @@ def test_noalloc_matches_plan_execute(cuda, dims, perm, es):
         plan.execute(inp.data_ptr(), ref.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(ref.cpu().numpy(), O.transpose_np(host, dims, perm, es).view(np.uint8))
-    for call in range(2):
-        out = torch.full_like(inp, 0x5A)
+    want = ref.cpu().numpy()
+    outs = [torch.full_like(inp, 0x5A) for _ in range(3)]
+    # a first call loads the library's module on this device if nothing has
+    # yet (the fixed array is device memory of the module, held from then on)
+    assert L.transpose_noalloc(dims, perm, es, stream, inp.data_ptr(),
+                               outs[2].data_ptr()) == L.LIBRETT_SUCCESS
+    torch.cuda.synchronize()
+    arena0, free0 = L.table_arena_stats(), torch.cuda.mem_get_info()[0]
+    for call, out in enumerate(outs[:2]):
         rc = L.transpose_noalloc(dims, perm, es, stream, inp.data_ptr(), out.data_ptr())
         assert rc == L.LIBRETT_SUCCESS, (call, rc)
         torch.cuda.synchronize()
-        assert torch.equal(out, ref), (dims, perm, es, call)
+        assert np.array_equal(out.cpu().numpy(), want), (dims, perm, es, call)
+    # no device memory was requested: the library's table arena is untouched
+    # and the device's free memory did not move
+    assert L.table_arena_stats() == arena0
+    assert torch.cuda.mem_get_info()[0] == free0
+
+
+@pytest.mark.parametrize("dims,perm,es,shift", [
+    ([4, 6, 64, 5, 32], [3, 0, 4, 2, 1], 4, 4),   # 16-byte units planned, pointers 4 bytes off
+    ([51, 2, 1354, 2, 9], [1, 3, 0, 2, 4], 8, 8),
+    ([201, 91, 63, 17], [2, 1, 3, 0], 4, 12),
+])
+def test_noalloc_unaligned_pointers(cuda, dims, perm, es, shift):
+    """Pointers aligned to the element but not to 16 bytes: the plan falls
+    back to element-size units (the register-staged pipeline, whose offset
+    tables live in shared memory) and still allocates nothing."""
+    import torch
+
+    rng = np.random.default_rng(sum(dims) + shift)
+    nb = int(np.prod(dims)) * es
+    host = rng.integers(0, 256, nb, dtype=np.uint8)
+    base_in = torch.zeros(nb + 64, dtype=torch.uint8, device="cuda")
+    base_in[shift:shift + nb] = torch.from_numpy(host).cuda()
+    ref = torch.zeros(nb + 64, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    ip = base_in.data_ptr() + shift
+    with L.Plan(dims, perm, es, stream) as plan:
+        plan.execute(ip, ref.data_ptr() + shift)
+    torch.cuda.synchronize()
+    want = O.transpose_np(host, dims, perm, es).view(np.uint8)
+    assert np.array_equal(ref[shift:shift + nb].cpu().numpy(), want)
+    outs = [torch.full_like(ref, 0x5A) for _ in range(3)]
+    assert L.transpose_noalloc(dims, perm, es, stream, ip,
+                               outs[2].data_ptr() + shift) == L.LIBRETT_SUCCESS
+    torch.cuda.synchronize()
+    arena0, free0 = L.table_arena_stats(), torch.cuda.mem_get_info()[0]
+    for call, out in enumerate(outs[:2]):
+        rc = L.transpose_noalloc(dims, perm, es, stream, ip, out.data_ptr() + shift)
+        assert rc == L.LIBRETT_SUCCESS, (call, rc)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        assert np.array_equal(got[shift:shift + nb], want), (dims, perm, es, call)
+        assert (got[:shift] == 0x5A).all() and (got[shift + nb:] == 0x5A).all()  # guard bands
+    assert L.table_arena_stats() == arena0
+    assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_bad_arguments(cuda):
