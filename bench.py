@@ -97,6 +97,22 @@ def problem_bytes(p):
     return int(np.prod(dims)) * es
 
 
+def line_dtype(problems):
+    return {4: "u32", 8: "u64", 16: "u128"}[problems[0][2]]
+
+
+def workload_config(args, problems):
+    """The `config` object, identical in the engine and reference lines of
+    a workload."""
+    return {"workload": WORKLOADS[args.workload] if args.workload != "custom"
+            else f"dims {problems[0][0]} perm {problems[0][1]} {problems[0][2]}-byte",
+            "problems": len(problems),
+            "suite_seed": SUITE_SEED if args.workload == "suite" else None,
+            "l2": "inputs larger than L2, no flush"
+            if max(problem_bytes(p) for p in problems) > 256 << 20
+            else "L2 flushed before every timed launch"}
+
+
 def load_peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -291,24 +307,30 @@ def run_reference(args):
         cpu_gather_time([problems[i % len(problems)]], 0.0, threads)
     if args.workload == "grouped":
         return _reference_grouped(args, problems, threads)
-    gbs_t, bytes_t = 0.0, 0
-    t_all = 0.0
+    # The K timed steps split the workload's problems into K consecutive
+    # slices (all 200 suite problems at K = 20, the same sample as the engine
+    # line's cpu_baseline); fewer problems than steps wrap around.
+    per = max(1, -(-len(problems) // args.steps))
+    bytes_t, t_all, timed = 0, 0.0, 0
     for i in range(args.steps):
-        p = problems[(args.warmup + i) % len(problems)]
-        gbs, _, t = cpu_gather_time([p], 0.0, threads)
+        sl = [problems[(i * per + k) % len(problems)] for k in range(per)]
+        _, n, t = cpu_gather_time(sl, float("inf"), threads)
         t_all += t
-        bytes_t += 2 * problem_bytes(p)
+        bytes_t += sum(2 * problem_bytes(p) for p in sl[:n])
+        timed += n
     value = bytes_t / t_all / 1e9
     line = {
         "impl": "reference", "metric": "effective GB/s (2*bytes/time)", "value": round(value, 3),
         "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(t_all / args.steps * 1e3, 3), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.workload == "suite" else "bits",
-        "data": "synthetic random 64-bit patterns",
-        "config": {"workload": WORKLOADS[args.workload], "problems_per_step": 1,
-                   "parallelism": "host threads"},
+        "scaling": "weak", "vs_baseline": None, "dtype": line_dtype(problems),
+        "data": "synthetic random 64-bit patterns, fixed seeds",
+        "config": workload_config(args, problems),
+        "parallelism": f"host threads x{threads}",
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"one suite problem per step, {args.steps} steps"},
+                         "sample": f"{timed} problems in {args.steps} steps of {per} consecutive "
+                                   f"problems (LibreTT has no CPU transpose: the oracle's host "
+                                   f"gather restates its algorithm)"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -359,6 +381,356 @@ def copy_ceiling(inp, out, stream, nbytes, reps=10):
             "bytes": nbytes, "how": f"best of {reps}, 2*bytes/time"}
 
 
+def link_ceiling(hin, hout, dbuf, dbuf2, nbytes, reps=5):
+    """Host-link ceilings for the end-to-end leg, measured in the same run:
+    pinned host -> device alone, device -> pinned host alone, and both at
+    once on two streams (copy engines); each the best of `reps`, GB/s of
+    bytes moved (both directions counted for the concurrent pair)."""
+    import torch
+
+    dev = dbuf.device
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def best(fn, moved):
+        fn()
+        torch.cuda.synchronize(dev)
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize(dev)
+            ev[0].record(s1)
+            s2.wait_event(ev[0])
+            fn()
+            j = torch.cuda.Event()
+            j.record(s2)
+            s1.wait_event(j)
+            ev[1].record(s1)
+            ev[1].synchronize()
+            ts.append(ev[0].elapsed_time(ev[1]))
+        return moved / (min(ts) / 1e3) / 1e9
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            dbuf[:nbytes].copy_(hin[:nbytes], non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s2):
+            hout[:nbytes].copy_(dbuf2[:nbytes], non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+
+    return {"h2d_gbs": round(best(h2d, nbytes), 1), "d2h_gbs": round(best(d2h, nbytes), 1),
+            "bidirectional_gbs": round(best(both, 2 * nbytes), 1), "bytes": nbytes,
+            "how": f"pinned host memory, copy engines, best of {reps}"}
+
+
+class DeviceData:
+    """Random 64-bit patterns in a device buffer, and an L2 flush buffer."""
+
+    def __init__(self, dev, nbytes, seed):
+        import torch
+
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        self.inp = torch.randint(-(2 ** 62), 2 ** 62, ((nbytes + 7) // 8,), dtype=torch.int64,
+                                 device=dev, generator=g).view(torch.uint8)[:nbytes]
+        self.out = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) \
+            if nbytes <= 256 << 20 else None
+
+
+def time_launches(fn, stream, steps, warmup, flush=None):
+    """Mean ms of fn() on `stream`: `steps` back-to-back launches between two
+    events after `warmup` untimed ones; with a flush buffer (inputs that fit
+    L2) every launch is timed alone after writing the buffer."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    if flush is None:
+        e[0].record(stream)
+        for _ in range(steps):
+            fn()
+        e[1].record(stream)
+        e[1].synchronize()
+        return e[0].elapsed_time(e[1]) / steps
+    total = 0.0
+    for _ in range(steps):
+        flush.zero_()
+        e[0].record(stream)
+        fn()
+        e[1].record(stream)
+        e[1].synchronize()
+        total += e[0].elapsed_time(e[1])
+    return total / steps
+
+
+def single_config_leg(name, dev, stream, peak, steps, warmup, cpu_budget):
+    """One of the single-problem configurations (C1, C3a, C3b) timed on the
+    device, verified on the device, with its own roofline, clocks and CPU
+    baseline."""
+    import librett_gb300 as L
+
+    prob = workload_problems(name, 1)[0]
+    dims, perm, es = prob
+    nb = problem_bytes(prob)
+    d = DeviceData(dev, nb, 99)
+    clocks = ClockSampler(dev.index or 0)
+    with L.Plan(dims, perm, es, stream) as pl:
+        clocks.start()
+        ms = time_launches(lambda: pl.execute(d.inp.data_ptr(), d.out.data_ptr()), stream, steps,
+                           warmup, d.flush)
+        clk = clocks.stop()
+        bad, _ = L.verify(dims, perm, es, d.inp.data_ptr(), d.out.data_ptr(), stream)
+        info = pl.info()
+    gbs = 2 * nb / (ms / 1e3) / 1e9
+    rec = {"workload": WORKLOADS[name], "bytes": nb, "ms": round(ms, 4), "gbs": round(gbs, 1),
+           "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(gbs / peak, 4)},
+           "method": L.METHOD_NAMES[info["method"]], "tile": info["tile_extent"],
+           "verified": bad == 0, "clocks": clk,
+           "l2": "flushed before every timed launch" if d.flush is not None else "inputs > L2"}
+    if cpu_budget > 0:
+        g, n, t = cpu_gather_time([prob], cpu_budget, host_threads())
+        rec["cpu_baseline"] = {"value": round(g, 3), "unit": "GB/s", "cores": host_threads(),
+                               "kind": "port", "sample": f"{n} host gather(s), {t:.2f} s"}
+    del d
+    return rec
+
+
+LIBRETT_SUITE = 40  # suite problems LibreTT's build is timed on beside the engine
+
+
+def librett_cuda_baseline(plan_cases, steps, warmup):
+    """LibreTT's own CUDA build as a baseline (the reference's GPU path, not
+    the thing measured): its unmodified sources compiled for sm_103a into
+    oracle/_ref/ref_driver by build() where they are present, run as a
+    separate process on this GPU through LibreTT's public API.  Times C1,
+    C3a, C3b and the first LIBRETT_SUITE suite problems with librettPlan and
+    with librettPlanMeasure (`steps` executes after `warmup`, CUDA events on
+    the plan's stream), and the planning latency of both on plan_cases.
+    Returns {"reason": ...} when the build is absent."""
+    import tempfile
+
+    drv = ROOT / "oracle" / "_ref" / "ref_driver"
+    if not drv.exists():
+        return {"reason": "LibreTT's CUDA build is absent on this machine: its sources were "
+                          "not present when build() ran"}
+    timed = ([("c1",) + tuple(workload_problems("c1", 1)[0]),
+              ("c3a",) + tuple(workload_problems("c3a", 1)[0]),
+              ("c3b",) + tuple(workload_problems("c3b", 1)[0])] +
+             [(f"suite{i}",) + tuple(p) for i, p in enumerate(suite_problems()[:LIBRETT_SUITE])])
+
+    def run(cases, st, wu, measure, env=None):
+        with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+            for _, dims, perm, es in cases:
+                f.write(" ".join(map(str, [len(dims), *dims, *perm, es, 2])) + "\n")
+            path = f.name
+        try:
+            res = subprocess.run([str(drv), "bench", path, str(st), str(wu), str(measure)],
+                                 capture_output=True, text=True, timeout=600,
+                                 env=dict(os.environ, **(env or {})))
+        finally:
+            os.unlink(path)
+        if res.returncode != 0:
+            raise RuntimeError(f"LibreTT driver exit {res.returncode}: {res.stderr[-300:]}")
+        return [json.loads(x) for x in res.stdout.splitlines() if x.startswith("{")]
+
+    try:
+        out = {"build": "LibreTT src/ unmodified, nvcc -O3 sm_103a (oracle/_ref/ref_driver)"}
+        for measure, key in ((0, "plan"), (1, "plan_measure")):
+            rows = run(timed, steps, warmup, measure)
+            for (name, *_), r in zip(timed, rows):
+                out.setdefault(name, {})[f"gbs_{key}"] = round(r["gbs"], 1)
+            suite = [r["gbs"] for (name, *_), r in zip(timed, rows) if name.startswith("suite")]
+            out.setdefault("suite40", {})[f"geomean_gbs_{key}"] = round(
+                float(np.exp(np.mean(np.log(suite)))), 1)
+        lat = {}
+        for measure, key in ((0, "librettPlan"), (1, "librettPlanMeasure")):
+            rows = run([("p",) + tuple(c) for c in plan_cases], 1, 0, measure)
+            lat[key] = round(statistics.median(r["plan_ms"] for r in rows) * 1e3, 1)
+        out["planning_us_median"] = lat
+        return out
+    except (RuntimeError, subprocess.TimeoutExpired, OSError) as e:
+        return {"reason": f"LibreTT's CUDA build did not run: {e}"}
+
+
+def grouped_leg(dev, stream, peak, steps, warmup, cpu_budget, nproblems=10000):
+    """The batched configuration: 10,000 transposes as one grouped execution
+    (one CUDA graph, the default tile policy) against the plain per-tensor
+    librettExecute loop on the same buffers, both timed here; every member's
+    output is then checked on the device."""
+    import torch
+
+    import librett_gb300 as L
+    from librett_gb300.workloads import packed_offsets
+
+    problems = workload_problems("grouped", nproblems)
+    offs, total = packed_offsets(problems)
+    d = DeviceData(dev, total, 4321)
+    ins = [d.inp.data_ptr() + o for o in offs]
+    outs = [d.out.data_ptr() + o for o in offs]
+    t0 = time.perf_counter()
+    plans = [L.Plan(dd, p, es, stream) for dd, p, es in problems]
+    plan_s = time.perf_counter() - t0
+    try:
+        t0 = time.perf_counter()
+        grp = L.Group(plans, ins, outs, stream)
+        create_s = time.perf_counter() - t0
+        ginfo = grp.info()
+        clocks = ClockSampler(dev.index or 0)
+        clocks.start()
+        ms = time_launches(grp.execute, stream, steps, warmup)
+        clk = clocks.stop()
+        loop_ms = time_launches(lambda: L.execute_batch(plans, ins, outs), stream, steps, warmup)
+        grp.execute()
+        torch.cuda.synchronize(dev)
+        ok = sum(L.verify(dd, p, es, i, o, stream)[0] == 0
+                 for (dd, p, es), i, o in zip(problems, ins, outs))
+        grp.destroy()
+    finally:
+        for pl in plans:
+            pl.destroy()
+    n = len(problems)
+    gbs = ginfo["bytes"] / (ms / 1e3) / 1e9
+    rec = {"workload": WORKLOADS["grouped"], "members": n, "bytes": ginfo["bytes"],
+           "transposes_per_s": round(n / (ms / 1e3), 1), "ms": round(ms, 4), "gbs": round(gbs, 1),
+           "loop": {"transposes_per_s": round(n / (loop_ms / 1e3), 1), "ms": round(loop_ms, 4),
+                    "what": "librettExecute on every plan in turn"},
+           "speedup_vs_loop": round(loop_ms / ms, 3),
+           "roofline": {"bound": "hbm", "achieved": round(gbs, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(gbs / peak, 4),
+                        "basis": "algorithmic bytes of the group / graph time"},
+           "buckets": ginfo["buckets"], "policy": "default (widest tiles, cp.async loads)",
+           "plan_s": round(plan_s, 3), "group_create_s": round(create_s, 3),
+           "verified": ok, "clocks": clk}
+    if cpu_budget > 0:
+        _, done, t = cpu_gather_time(problems, cpu_budget, host_threads())
+        rec["cpu_baseline"] = {"value": round(done / t, 1), "unit": "transposes/s",
+                               "cores": host_threads(), "kind": "port",
+                               "sample": f"first {done} members, {t:.2f} s of host gather"}
+    del d
+    return rec
+
+
+def planning_leg(dev, stream, cases):
+    """Planning latency on held-out problems of the plan-selection
+    distribution: a cold librettPlan (learned selector, plan cache off) and
+    librettPlanMeasure, each a C-ABI call plus a stream synchronise, median
+    over the problems."""
+    import ctypes
+
+    import torch
+
+    import librett_gb300 as L
+    from librett_gb300 import _lib
+
+    lib = _lib.load()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    maxb = max(problem_bytes(c) for c in cases)
+    d = DeviceData(dev, maxb, 5)
+    prev_sel = lib.librett_c_set_plan_selector(0)
+    prev_cache = lib.librett_c_set_plan_cache(0)
+    plan_us, meas_us, learned = [], [], 0
+    try:
+        for dims, perm, es in cases:
+            dc, pc = _lib.int_array(dims), _lib.int_array(perm)
+            torch.cuda.synchronize(dev)
+            h = ctypes.c_uint(0)
+            t0 = time.perf_counter()
+            rc = lib.librett_c_plan(ctypes.byref(h), len(dims), dc, pc, es, sptr)
+            torch.cuda.current_stream(dev).synchronize()
+            plan_us.append((time.perf_counter() - t0) * 1e6)
+            assert rc == 0, rc
+            learned += L.plan_info(h.value)["selected_by"] == 1
+            lib.librett_c_destroy(h.value)
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            rc = lib.librett_c_plan_measure(ctypes.byref(h), len(dims), dc, pc, es, sptr,
+                                            d.inp.data_ptr(), d.out.data_ptr())
+            torch.cuda.current_stream(dev).synchronize()
+            meas_us.append((time.perf_counter() - t0) * 1e6)
+            assert rc == 0, rc
+            lib.librett_c_destroy(h.value)
+    finally:
+        lib.librett_c_set_plan_selector(prev_sel)
+        lib.librett_c_set_plan_cache(prev_cache)
+    a, b = statistics.median(plan_us), statistics.median(meas_us)
+    return {"problems": len(cases), "librettPlan_us_median": round(a, 1),
+            "librettPlanMeasure_us_median": round(b, 1), "ratio": round(b / a, 2),
+            "learned_picks": learned,
+            "how": "C-ABI call + stream synchronise from Python (ctypes), plan cache off"}
+
+
+def _time_candidate(pl, ip, op, stream, e):
+    """Median of three event-timed batches of >= ~150 us of executes (ms)."""
+    nb = problem_bytes((pl.dim, pl.permutation, pl.sizeofType))
+    reps = int(min(64, max(1, np.ceil(150e-6 / (2.0 * nb / 5e12 + 4e-6)))))
+    pl.execute(ip, op)
+    ts = []
+    for _ in range(3):
+        e[0].record(stream)
+        for _ in range(reps):
+            pl.execute(ip, op)
+        e[1].record(stream)
+        e[1].synchronize()
+        ts.append(e[0].elapsed_time(e[1]) / reps)
+    return float(np.median(ts))
+
+
+def selection_leg(dev, stream, cases):
+    """Plan-choice regret on held-out problems: every candidate of the
+    default set is timed, then the learned pick and the analytic pick are
+    compared with the fastest (regret = t(pick) / t(best) - 1, geomean over
+    problems)."""
+    import ctypes
+
+    import torch
+
+    import librett_gb300 as L
+    from librett_gb300 import _lib
+
+    lib = _lib.load()
+    maxb = max(problem_bytes(c) for c in cases)
+    d = DeviceData(dev, maxb, 6)
+    ip, op = d.inp.data_ptr(), d.out.data_ptr()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    prev_sel = lib.librett_c_set_plan_selector(0)
+    prev_cache = lib.librett_c_set_plan_cache(0)
+    ratios = {"learned": [], "analytic": []}
+    try:
+        for dims, perm, es in cases:
+            picks = {}
+            for mode, name in ((2, "learned"), (1, "analytic")):
+                lib.librett_c_set_plan_selector(mode)
+                with L.Plan(dims, perm, es, stream) as pl:
+                    picks[name] = pl.info()["candidate"]
+                    ncand = pl.info()["num_candidates"]
+            lib.librett_c_set_plan_selector(0)
+            times = []
+            for c in range(ncand):
+                with L.Plan(dims, perm, es, stream, candidate=c) as pl:
+                    times.append(_time_candidate(pl, ip, op, stream, e))
+            best = min(times)
+            for name in ratios:
+                ratios[name].append(times[picks[name]] / best)
+    finally:
+        lib.librett_c_set_plan_selector(prev_sel)
+        lib.librett_c_set_plan_cache(prev_cache)
+    g = {k: float(np.exp(np.mean(np.log(v)))) - 1 for k, v in ratios.items()}
+    p90 = {k: float(np.percentile(v, 90)) - 1 for k, v in ratios.items()}
+    return {"problems": len(cases),
+            "regret_geomean": {k: round(v, 4) for k, v in g.items()},
+            "regret_p90": {k: round(v, 4) for k, v in p90.items()},
+            "exact_best": {k: int(sum(abs(x - 1) < 1e-9 for x in v)) for k, v in ratios.items()},
+            "how": "every default candidate timed (median of 3 event-timed batches), "
+                   "regret = t(pick)/t(best) - 1"}
+
+
 def run_engine(args):
     import torch
 
@@ -379,9 +751,13 @@ def run_engine(args):
     infos = [pl.info() for pl in plans]
     ip, op = inp.data_ptr(), out.data_ptr()
     step_bytes = sum(2 * problem_bytes(p) for p in problems)
+    # inputs that fit L2: flush it before every launch, time the launches alone
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if maxb <= 256 << 20 else None
 
     def step(events=None):
         for k, pl in enumerate(plans):
+            if flush is not None:
+                flush.zero_()
             if events is not None:
                 events[k][0].record(stream)
             pl.execute(ip, op)
@@ -409,8 +785,20 @@ def run_engine(args):
     barrier(world)
     clk = clocks.stop()
     ms = t0.elapsed_time(t1)
+    if flush is not None:  # the launches only, without the flushes between them
+        ms = sum(e0.elapsed_time(e1) for evs in ev for e0, e1 in evs)
     ms_max = max_over_ranks(ms, world)
     value = world * step_bytes * args.steps / (ms_max / 1e3) / 1e9
+
+    # every problem's output checked on the device (LibreTT's bench checks
+    # every shape it times, tests/librett_bench.cpp:866)
+    verified = None
+    if not args.no_verify:
+        verified = 0
+        for (dims, perm, es), pl in zip(problems, plans):
+            out.fill_(0xA5)
+            pl.execute(ip, op)
+            verified += L.verify(dims, perm, es, ip, op, stream)[0] == 0
 
     # per-kernel breakdown from the per-launch events
     per_kernel = {}
@@ -502,12 +890,28 @@ def run_engine(args):
         e2e = {"value": round(world * step_bytes / (ems / 1e3) / 1e9, 3), "unit": "GB/s",
                "h2d_bytes_per_step": step_bytes // 2, "d2h_bytes_per_step": step_bytes // 2,
                "ms_per_step": round(ems, 3)}
+        if maxb >= 1 << 26:
+            link = link_ceiling(hin, hout, d_in[1], d_out[1], maxb)
+            link["e2e_frac_of_bidirectional"] = round(
+                e2e["value"] / world / link["bidirectional_gbs"], 4)
+            e2e["link_ceiling_same_run"] = link
+        del hin, hout, d_in, d_out
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         gbs, n, t = cpu_gather_time(problems, args.cpu_budget, host_threads())
         cpu = {"value": round(gbs, 3), "unit": "GB/s", "cores": host_threads(), "kind": "port",
                "sample": f"first {n} problem(s) of the workload, {t:.1f} s of host gather"}
+
+    # the other configurations, each timed and checked in this run (1 GPU)
+    configs = None
+    if args.workload == "suite" and world == 1 and not args.no_extras:
+        for pl in plans:
+            pl.destroy()
+        plans = []
+        del inp, out
+        torch.cuda.empty_cache()
+        configs = extra_legs(args, dev, stream, peak)
 
     if rank != 0:
         return 0
@@ -526,14 +930,13 @@ def run_engine(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {4: "u32", 8: "u64", 16: "u128"}[problems[0][2]],
+        "dtype": line_dtype(problems),
         "data": "synthetic random 64-bit patterns, fixed seeds",
-        "config": {"workload": WORKLOADS[args.workload] if args.workload != "custom"
-                   else f"dims {problems[0][0]} perm {problems[0][1]} {problems[0][2]}-byte",
-                   "problems": len(problems), "candidate": args.candidate,
-                   "suite_seed": SUITE_SEED if args.workload == "suite" else None,
-                   "bytes_per_step": step_bytes, "l2": "inputs larger than L2, no flush",
-                   "parallelism": f"replicas x{world}", "methods": methods},
+        "config": workload_config(args, problems),
+        "parallelism": f"replicas x{world}",
+        "details": {"bytes_per_step": step_bytes, "candidate": args.candidate,
+                    "methods": methods},
+        "verified": verified,
         "geomean_gbs": round(geo, 3),
         "geomean_frac_of_copy": round(geo / peak, 4),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 3),
@@ -549,11 +952,42 @@ def run_engine(args):
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk,
+        "configs": configs,
     }
     print(json.dumps(line), flush=True)
     for pl in plans:
         pl.destroy()
     return 0
+
+
+def extra_legs(args, dev, stream, peak):
+    """C1, C3a, C3b, the grouped batch, planning latency and plan-choice
+    regret, each measured in this run, plus LibreTT's CUDA build on C1, C3a,
+    C3b and the first suite problems when it is present."""
+    from librett_gb300.learn.data import problems as selector_problems
+
+    held_out = selector_problems(args.planning_problems, 424242)  # not used in training
+    out = {}
+    for name in ("c1", "c3a", "c3b"):
+        out[name] = single_config_leg(name, dev, stream, peak, 20, 5, args.extra_cpu_budget)
+    out["grouped"] = grouped_leg(dev, stream, peak, 5, 3, args.extra_cpu_budget,
+                                 args.grouped_problems)
+    out["planning"] = planning_leg(dev, stream, held_out)
+    out["selection"] = selection_leg(dev, stream, held_out[:args.selection_problems])
+    ref = librett_cuda_baseline(held_out, 10, 3)
+    out["librett_cuda"] = ref
+    if "reason" not in ref:
+        for name in ("c1", "c3a", "c3b"):
+            r = ref.get(name, {})
+            if r.get("gbs_plan"):
+                out[name]["vs_librett_plan"] = round(out[name]["gbs"] / r["gbs_plan"], 3)
+                out[name]["vs_librett_plan_measure"] = round(
+                    out[name]["gbs"] / r["gbs_plan_measure"], 3)
+        lat = ref.get("planning_us_median", {})
+        if lat.get("librettPlanMeasure"):
+            out["planning"]["vs_librett_plan_measure"] = round(
+                lat["librettPlanMeasure"] / out["planning"]["librettPlan_us_median"], 2)
+    return out
 
 
 def run_grouped(args):
@@ -795,6 +1229,19 @@ def main(argv=None):
                     help="seconds of host gather for the cpu_baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-verify", action="store_true",
+                    help="skip the device check of every problem's output after timing")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="suite workload: skip the other configurations (C1, C3a, C3b, grouped, "
+                         "planning, selection, LibreTT's CUDA build)")
+    ap.add_argument("--extra-cpu-budget", type=float, default=2.0,
+                    help="seconds of host gather for each extra configuration's cpu_baseline")
+    ap.add_argument("--selection-problems", type=int, default=100,
+                    help="held-out problems whose every candidate is timed for the regret")
+    ap.add_argument("--planning-problems", type=int, default=200,
+                    help="held-out problems of the plan-selection distribution for planning latency")
+    ap.add_argument("--grouped-problems", type=int, default=10000,
+                    help="members of the batched configuration in the suite line's extras")
     ap.add_argument("--buckets", type=str, default=None,
                     help="grouped workload: write the graph's bucket launches (JSON lines)")
     ap.add_argument("--policy", type=str, default=None,

@@ -6,8 +6,15 @@ the analytic model (plan cache off), of librettPlanMeasure (which times
 every candidate), and of a repeated librettPlan served by the plan cache;
 and the measured execute time of the learned and the analytic choice.
 
+With --all-candidates every candidate of the default set is timed too, so
+each selector's regret against the measured best is known per problem; with
+--librett-choice (oracle/ref_bench/run_ref.py --choice output for the same
+problems and seed) LibreTT's analytic GpuModel pick (its librettPlan) and its
+librettPlanMeasure pick are joined per problem.
+
 Usage (on a GPU):
-    python -m librett_gb300.learn.evaluate --problems 200 --seed 424242 --out eval.json
+    python -m librett_gb300.learn.evaluate --problems 200 --seed 424242 --out eval.json \
+        [--all-candidates] [--librett-choice reference_choice.json]
 """
 from __future__ import annotations
 
@@ -41,7 +48,7 @@ def _time_exec(plan, din, dout, stream, ev):
     return float(np.median(ts))
 
 
-def evaluate(probs):
+def evaluate(probs, all_candidates=False):
     import torch
 
     lib = _lib.load()
@@ -86,6 +93,16 @@ def evaluate(probs):
             plan = L.Plan(dims, perm, es, stream, measure=(a.data_ptr(), b.data_ptr()))
             r["exec_ms_measure"] = _time_exec(plan, a.data_ptr(), b.data_ptr(), stream, ev) * 1e3
             plan.destroy()
+            if all_candidates:
+                lib.librett_c_set_plan_selector(0)
+                times = []
+                for c in range(info["num_candidates"]):
+                    plan = L.Plan(dims, perm, es, stream, candidate=c)
+                    times.append(_time_exec(plan, a.data_ptr(), b.data_ptr(), stream, ev) * 1e3)
+                    plan.destroy()
+                r["exec_ms_candidates"] = times
+                r["exec_ms_best"] = min(times + [r["exec_ms_learned"], r["exec_ms_analytic"],
+                                                 r["exec_ms_measure"]])
             # a repeated shape with the plan cache on (the second call hits)
             lib.librett_c_set_plan_selector(0)
             lib.librett_c_set_plan_cache(16)
@@ -124,7 +141,47 @@ def evaluate(probs):
                 "learned_ms": float(np.median([r["plan_ms_learned"] for r in sel])),
                 "measure_ms": float(np.median([r["plan_ms_measure"] for r in sel]))}
     summary["by_size"] = buckets
+    if all_candidates:
+        summary["regret_vs_best"] = {
+            k: _regret([r[f"exec_ms_{k}"] / r["exec_ms_best"] for r in rows])
+            for k in ("learned", "analytic", "measure")}
     return summary, rows
+
+
+def _regret(ratios):
+    """Geomean and p90 of t(pick) / t(best) - 1."""
+    ratios = np.asarray(ratios, dtype=np.float64)
+    return {"geomean": float(np.exp(np.mean(np.log(ratios)))) - 1,
+            "p90": float(np.percentile(ratios, 90)) - 1,
+            "exact_best": int(np.sum(ratios <= 1 + 1e-9))}
+
+
+def join_librett(summary, rows, choice):
+    """Adds LibreTT's per-problem picks (its librettPlan = the GpuModel
+    choice, and its librettPlanMeasure choice) to the rows and the regret
+    table: GpuModel's regret against LibreTT's own measured choice, and both
+    LibreTT picks against the engine's measured best."""
+    plan, meas = choice["plan"], choice["measure"]
+    assert len(plan) == len(rows) == len(meas)
+    for r, p, m in zip(rows, plan, meas):
+        assert p["dims"] == r["dims"] and p["perm"] == r["perm"] and p["es"] == r["es"]
+        r["librett_exec_ms_plan"] = p["ms"]
+        r["librett_exec_ms_measure"] = m["ms"]
+        r["librett_plan_ms"] = p["plan_ms"]
+        r["librett_plan_measure_ms"] = m["plan_ms"]
+    summary["librett"] = {
+        "gpumodel_regret_vs_librett_measure": _regret(
+            [max(1.0, r["librett_exec_ms_plan"] / r["librett_exec_ms_measure"]) for r in rows]),
+        "plan_ms_median": {"librettPlan": float(np.median([r["librett_plan_ms"] for r in rows])),
+                           "librettPlanMeasure": float(np.median(
+                               [r["librett_plan_measure_ms"] for r in rows]))},
+    }
+    if "exec_ms_best" in rows[0]:
+        summary["librett"]["gpumodel_vs_engine_best"] = _regret(
+            [r["librett_exec_ms_plan"] / r["exec_ms_best"] for r in rows])
+        summary["librett"]["librett_measure_vs_engine_best"] = _regret(
+            [r["librett_exec_ms_measure"] / r["exec_ms_best"] for r in rows])
+    return summary
 
 
 def main(argv=None):
@@ -132,11 +189,18 @@ def main(argv=None):
     ap.add_argument("--problems", type=int, default=200)
     ap.add_argument("--seed", type=int, default=424242)
     ap.add_argument("--out", default=None)
+    ap.add_argument("--all-candidates", action="store_true",
+                    help="time every candidate of every problem (regret against the best)")
+    ap.add_argument("--librett-choice", default=None,
+                    help="run_ref.py --choice output for the same problems: join LibreTT's picks")
     args = ap.parse_args(argv)
     import torch
 
     torch.cuda.set_device(0)
-    summary, rows = evaluate(problems(args.problems, args.seed))
+    summary, rows = evaluate(problems(args.problems, args.seed), args.all_candidates)
+    if args.librett_choice:
+        with open(args.librett_choice) as f:
+            summary = join_librett(summary, rows, json.load(f))
     print(json.dumps(summary, indent=1))
     if args.out:
         with open(args.out, "w") as f:

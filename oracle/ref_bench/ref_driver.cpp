@@ -16,12 +16,19 @@
 //   ref_driver loop <cases> <steps> <warmup>
 //       plan every case, then time the per-tensor loop (librettExecute on
 //       every case in turn, each tensor at its own offset of one buffer);
-//       print one JSON line.
+//       print one JSON line;
+//   ref_driver random <cases>
+//       for each case (kind 3), fill the input on the device with the
+//       seeded random words of oracle/vectors.py, plan with librettPlan,
+//       execute, and write the output to standard output as an 8-byte
+//       little-endian length followed by the bytes (the caller digests it).
 //
 // Case file: one case per line, "rank d0 .. d{r-1} p0 .. p{r-1} es kind"
-// (kind 0 = value pattern, 1 = word pattern, 2 = leave memory as is).
+// (kind 0 = value pattern, 1 = word pattern, 2 = leave memory as is,
+// 3 = seeded random words; kind 3 is followed by the 64-bit key).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <complex>
 #include <cstdio>
@@ -40,6 +47,7 @@ struct Case {
   std::vector<int> dim, perm;
   int es = 8;
   int kind = 0;
+  unsigned long long key = 0;  // kind 3
 };
 
 std::vector<Case> readCases(const char* path) {
@@ -56,6 +64,7 @@ std::vector<Case> readCases(const char* path) {
     for (int i = 0; i < r; ++i) is >> c.dim[i];
     for (int i = 0; i < r; ++i) is >> c.perm[i];
     is >> c.es >> c.kind;
+    if (c.kind == 3) is >> c.key;
     out.push_back(c);
   }
   return out;
@@ -92,6 +101,64 @@ void fillHost(const Case& c, std::vector<unsigned char>& buf) {
     std::complex<double>* p = reinterpret_cast<std::complex<double>*>(buf.data());
     for (size_t i = 0; i < vol; ++i) p[i] = std::complex<double>((double)i, 0.0);
   }
+}
+
+// Word i of a seeded random input: SplitMix64's output function of
+// key + (i + 1) * golden ratio (the definition in oracle/vectors.py).
+__global__ void fillRandomKernel(unsigned long long* w, size_t n, unsigned long long key) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long z = key + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    w[i] = z ^ (z >> 31);
+  }
+}
+
+int randomMode(const char* casePath) {
+  std::vector<Case> cases = readCases(casePath);
+  size_t maxBytes = 0;
+  for (auto& c : cases) maxBytes = std::max(maxBytes, volumeOf(c) * c.es);
+  const size_t maxWords = (maxBytes + 7) / 8;
+  unsigned long long* din;
+  void* dout;
+  CHECK(cudaMalloc(&din, maxWords * 8));
+  CHECK(cudaMalloc(&dout, maxBytes));
+  unsigned char* host = nullptr;
+  CHECK(cudaMallocHost(&host, maxBytes));
+  cudaStream_t s;
+  CHECK(cudaStreamCreate(&s));
+  for (size_t n = 0; n < cases.size(); ++n) {
+    Case& c = cases[n];
+    if (c.kind != 3) {
+      std::fprintf(stderr, "case %zu: random mode needs kind 3\n", n);
+      return 3;
+    }
+    const size_t bytes = volumeOf(c) * c.es;
+    fillRandomKernel<<<1024, 256, 0, s>>>(din, (bytes + 7) / 8, c.key);
+    CHECK(cudaGetLastError());
+    CHECK(cudaMemsetAsync(dout, 0xA5, bytes, s));
+    librettHandle h;
+    librettResult r = librettPlan(&h, (int)c.dim.size(), c.dim.data(), c.perm.data(), c.es, s);
+    if (r == LIBRETT_SUCCESS) r = librettExecute(h, din, dout);
+    if (r != LIBRETT_SUCCESS) {
+      std::fprintf(stderr, "case %zu: plan/execute -> %d\n", n, (int)r);
+      return 3;
+    }
+    CHECK(cudaStreamSynchronize(s));
+    CHECK(cudaMemcpy(host, dout, bytes, cudaMemcpyDeviceToHost));
+    librettDestroy(h);
+    unsigned char len[8];
+    for (int b = 0; b < 8; ++b) len[b] = (unsigned char)((unsigned long long)bytes >> (8 * b));
+    if (std::fwrite(len, 1, 8, stdout) != 8 || std::fwrite(host, 1, bytes, stdout) != bytes)
+      return 4;
+    std::fflush(stdout);
+  }
+  CHECK(cudaFreeHost(host));
+  CHECK(cudaFree(din));
+  CHECK(cudaFree(dout));
+  CHECK(cudaStreamDestroy(s));
+  return 0;
 }
 
 int golden(const char* casePath, const char* outDir) {
@@ -252,10 +319,11 @@ int main(int argc, char** argv) {
   if (argc >= 5 && std::strcmp(argv[1], "loop") == 0)
     return loop(argv[2], std::atoi(argv[3]), std::atoi(argv[4]));
   if (argc >= 4 && std::strcmp(argv[1], "golden") == 0) return golden(argv[2], argv[3]);
+  if (argc >= 3 && std::strcmp(argv[1], "random") == 0) return randomMode(argv[2]);
   if (argc >= 6 && std::strcmp(argv[1], "bench") == 0)
     return bench(argv[2], std::atoi(argv[3]), std::atoi(argv[4]), std::atoi(argv[5]));
   std::fprintf(stderr,
                "usage: ref_driver golden <cases> <outdir> | bench <cases> <steps> <warmup> "
-               "<measure> | loop <cases> <steps> <warmup>\n");
+               "<measure> | loop <cases> <steps> <warmup> | random <cases>\n");
   return 1;
 }

@@ -44,10 +44,34 @@ def _common(b, steps, warmup):
 
 
 def test_suite_line():
-    b = _line("--steps", "3", "--warmup", "3", "--problems", "4", "--no-cpu")
+    b = _line("--steps", "3", "--warmup", "3", "--problems", "4", "--no-cpu", "--no-extras")
     _common(b, 3, 3)
     assert b["unit"] == "GB/s" and b["gpu_launches"] == 3 * 4
     assert 0 < b["geomean_frac_of_copy"] < 1.5
+    assert b["verified"] == 4
+    link = b["e2e"]["link_ceiling_same_run"]
+    assert link["h2d_gbs"] > 0 and link["d2h_gbs"] > 0 and link["bidirectional_gbs"] > 0
+
+
+def test_suite_line_with_the_other_configurations():
+    """The default line also carries C1, C3a, C3b, the grouped batch,
+    planning latency and plan-choice regret, each measured in the run (here
+    on reduced counts)."""
+    b = _line("--steps", "3", "--warmup", "3", "--problems", "2", "--no-cpu",
+              "--grouped-problems", "300", "--planning-problems", "12",
+              "--selection-problems", "6", "--extra-cpu-budget", "0.2")
+    c = b["configs"]
+    for name in ("c1", "c3a", "c3b"):
+        assert c[name]["verified"] is True and c[name]["gbs"] > 0
+        r = c[name]["roofline"]
+        assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-3
+        assert c[name]["cpu_baseline"]["value"] > 0
+    g = c["grouped"]
+    assert g["verified"] == g["members"] == 300 and g["speedup_vs_loop"] > 1
+    assert c["planning"]["problems"] == 12 and c["planning"]["ratio"] > 1
+    assert c["selection"]["problems"] == 6
+    assert set(c["selection"]["regret_geomean"]) == {"learned", "analytic"}
+    assert "reason" in c["librett_cuda"] or c["librett_cuda"]["c3a"]["gbs_plan"] > 0
 
 
 def test_grouped_line():
