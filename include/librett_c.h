@@ -46,7 +46,9 @@ typedef struct librett_plan_info {
   int slots;                       /* elements (or units) per thread per tile     */
   int smem_bytes;                  /* dynamic shared memory per CTA               */
   int pad_shift;                   /* smem padding: 1 element per 2^pad_shift    */
-  int pipeline;                    /* tile: 0 register-staged, 1 cp.async ring   */
+  int pipeline;                    /* tile: 0 register-staged, 1 cp.async ring,
+                                      2 one tile per CTA, 3 the same with bulk
+                                      copies (cp.async.bulk + mbarrier)        */
   int unit_in_bytes;               /* global load width                           */
   int unit_out_bytes;              /* global store width                          */
   int run_in_bytes;                /* contiguous input run per tile               */
@@ -81,6 +83,13 @@ int librett_c_destroy(librettHandle handle);
 /* Plan introspection; no LibreTT counterpart (LibreTT prints it with
  * librettPlan_t::print, src/plan.cpp:825-833). */
 int librett_c_plan_info(librettHandle handle, librett_plan_info* info);
+
+/* Device status word of a plan, read after the plan's stream has drained
+ * (synchronises it): 0, or bit 0 set when a launch of the bulk-copy
+ * pipeline (pipeline 3) waited longer than its limit for its copies and
+ * skipped its stores.  Plans of other pipelines always read 0.  No LibreTT
+ * counterpart (LibreTT exits on device errors, src/GpuUtils.h:47-56). */
+int librett_c_plan_status(librettHandle handle, unsigned* status);
 
 /* Host-only planning without a device or a handle: runs the same input check,
  * rank fusion and tile choice as librett_c_plan for a device with `num_sms`
@@ -216,6 +225,17 @@ int librett_c_execute_grouped(int count, const librettHandle* plans, void* const
  * bad problem or candidate. */
 int librett_c_group_run_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
                               int num_sms, int candidate, int element_units);
+
+/* Host-only self-check of the bulk-copy pipeline for candidate `candidate`
+ * of the planner's candidate list (candidate set 1): every segment the
+ * kernel copies with one cp.async.bulk must be contiguous in global memory
+ * (per the load-unit table) and in shared memory (between padding gaps),
+ * 16-byte aligned in both, and the segments must cover the tile.  Returns
+ * LIBRETT_SUCCESS, LIBRETT_INTERNAL_ERROR on a violation,
+ * LIBRETT_INVALID_DEVICE when the candidate is not a bulk-copy tile,
+ * LIBRETT_INVALID_PARAMETER for a bad problem or candidate. */
+int librett_c_bulk_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                         int num_sms, int candidate);
 
 /* The plain per-tensor loop the grouped path replaces: librettExecute on
  * each (plan, idata, odata) in order, one launch each; stops at and returns

@@ -129,7 +129,7 @@ class Group:
 
     # policies per member size class (librett_c.h): tile + 4 * loads
     POLICY_SELECTOR, POLICY_WIDE, POLICY_WIDEST, POLICY_FILL = 0, 1, 2, 3
-    LOADS_REGISTERS, LOADS_ASYNC, LOADS_RUNS = 0, 4, 8
+    LOADS_REGISTERS, LOADS_ASYNC = 0, 4
 
     def __init__(self, plans, idata, odata, stream=None, *, policy=None):
         n, hs, ins, outs = _handle_arrays(plans, idata, odata)
@@ -309,6 +309,15 @@ class Plan:
 
     def info(self) -> dict:
         return plan_info(self.handle)
+
+    def status(self) -> int:
+        """The plan's device status word (librett_c_plan_status): 0, or bit
+        0 when a bulk-copy launch gave up waiting for its copies."""
+        st = ctypes.c_uint(0)
+        rc = _lib.load().librett_c_plan_status(self.handle, ctypes.byref(st))
+        if rc != LIBRETT_SUCCESS:
+            raise LibrettError(rc, "librett_c_plan_status")
+        return st.value
 
     def destroy(self) -> None:
         if self.handle is not None:

@@ -136,6 +136,9 @@ C_FUNCTIONS = [
     ("librett_c_group_run_check", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
       ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("librett_c_bulk_check", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
+      ctypes.c_int, ctypes.c_int]),
     ("librett_c_execute_batch", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     ("librett_c_group_info", ctypes.c_int,
@@ -147,6 +150,7 @@ C_FUNCTIONS = [
      [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
       ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_inject_fault", ctypes.c_int, [ctypes.c_int, ctypes.c_longlong]),
+    ("librett_c_plan_status", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint)]),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]
 

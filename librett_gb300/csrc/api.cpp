@@ -424,6 +424,40 @@ int librett_c_describe(int rank, const int* dim, const int* permutation, size_t 
   return LIBRETT_SUCCESS;
 }
 
+int librett_c_bulk_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
+                         int num_sms, int candidate) {
+  if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
+  lt::Fused f;
+  lt::fuseRanks(rank, dim, permutation, (int)sizeofType, f);
+  const int sms = num_sms > 0 ? num_sms : 152;
+  std::vector<lt::PlanDesc> cands = lt::enumerateCandidates(f, sms, true);
+  if (candidate < 0 || candidate >= (int)cands.size()) return LIBRETT_INVALID_PARAMETER;
+  lt::PlanDesc pd = cands[candidate];
+  if (!lt::refineCandidate(pd, sms)) return LIBRETT_INTERNAL_ERROR;
+  if (pd.kernel != lt::K_TILE || pd.pipe != lt::PIPE_BULK) return LIBRETT_INVALID_DEVICE;
+  const lt::TileParams& tp = pd.tile;
+  const int L = tp.segLen, es = (int)sizeofType;
+  if (L <= 0 || L % tp.lv || tp.tileVol % L || tp.lv * es != 16 || (L * es) % 16)
+    return LIBRETT_INTERNAL_ERROR;
+  std::vector<int> ldOff(tp.nIn), stOff(tp.nOut);
+  std::vector<unsigned short> stSm(tp.tileVol);
+  lt::tileTablesHost(tp, ldOff.data(), stOff.data(), stSm.data());
+  auto pad = [&](int j) { return j + ((j >> tp.padShift) << tp.padLog); };
+  // every segment is one contiguous piece of global memory and of shared
+  // memory, starts 16-byte aligned in both, and the segments tile the tile
+  for (int j0 = 0; j0 < tp.tileVol; j0 += L) {
+    const int u0 = j0 / tp.lv;
+    if (((long long)ldOff[u0] * es) % 16 || ((long long)pad(j0) * es) % 16)
+      return LIBRETT_INTERNAL_ERROR;
+    for (int j = j0; j < j0 + L; j += tp.lv) {
+      if (ldOff[j / tp.lv] != ldOff[u0] + (j - j0)) return LIBRETT_INTERNAL_ERROR;
+      if (pad(j) != pad(j0) + (j - j0)) return LIBRETT_INTERNAL_ERROR;
+    }
+  }
+  if (pad(tp.tileVol - 1) >= tp.smStride) return LIBRETT_INTERNAL_ERROR;
+  return LIBRETT_SUCCESS;
+}
+
 int librett_c_group_run_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
                               int num_sms, int candidate, int element_units) {
   if (lt::checkInput(rank, dim, permutation, sizeofType) != 0) return LIBRETT_INVALID_PARAMETER;
@@ -573,5 +607,18 @@ int librett_c_inject_fault(int site, long long after) {
 
 int librett_c_table_arena_stats(long long* slab_bytes, long long* blocks, long long* pool_bytes) {
   lt::tableArenaStats(slab_bytes, blocks, pool_bytes);
+  return LIBRETT_SUCCESS;
+}
+
+int librett_c_plan_status(librettHandle handle, unsigned* status) {
+  if (status == nullptr) return LIBRETT_INVALID_PARAMETER;
+  std::shared_ptr<PlanObj> obj = lt::findPlan(handle);
+  if (!obj) return LIBRETT_INVALID_PLAN;
+  *status = 0;
+  if (obj->tables.status == nullptr) return LIBRETT_SUCCESS;
+  if (cudaMemcpyAsync(status, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                      obj->stream) != cudaSuccess ||
+      cudaStreamSynchronize(obj->stream) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
   return LIBRETT_SUCCESS;
 }

@@ -231,8 +231,8 @@ cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, int loads, const G
 bool pickTile(const Member& m, int policy, int sms, const std::string& dev, PlanDesc& out) {
   policy %= GP_TILES;
   const PlanDesc& own = m.plan->pd;
-  if (policy == GP_SELECTOR && own.kernel == K_TILE && own.pipe == PIPE_FLAT) {
-    out = own;
+  if (policy == GP_SELECTOR && own.kernel == K_TILE && flatTables(own.pipe)) {
+    out = own;  // the group uses the tile geometry only
   } else {
     // the selector ranks screened candidates (as for librettPlan)
     std::vector<PlanDesc> c =

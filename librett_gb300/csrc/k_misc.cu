@@ -121,8 +121,9 @@ struct TableParams {
 
 __global__ void __launch_bounds__(256)
 writeTileTablesKernel(const __grid_constant__ TableParams p, int* ldOff, int* stOff,
-                      unsigned short* stSm) {
+                      unsigned short* stSm, unsigned* status) {
   const int stride = gridDim.x * blockDim.x;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *status = 0;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < p.nIn; u += stride) {
     int rem = u * p.lv, off = 0;
     for (int t = 0; t < p.nTR; ++t) {
@@ -154,7 +155,11 @@ size_t deviceTableBytes(const TileParams& tp, size_t* stOffset, size_t* smOffset
   // 16-byte aligned
   *stOffset = 4 * (size_t)tp.nIn;
   *smOffset = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16;
-  return *smOffset + 2 * (size_t)tp.tileVol;
+  return statusOffset(tp, *smOffset) + 16;
+}
+
+size_t statusOffset(const TileParams& tp, size_t smOffset) {
+  return ((smOffset + 2 * (size_t)tp.tileVol + 15) / 16) * 16;
 }
 
 cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStream_t s,
@@ -164,6 +169,7 @@ cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStr
   int* ld = reinterpret_cast<int*>(base);
   int* st = reinterpret_cast<int*>(base + stOffset);
   unsigned short* sm = reinterpret_cast<unsigned short*>(base + smOffset);
+  unsigned* status = reinterpret_cast<unsigned*>(base + statusOffset(tp, smOffset));
   TableParams p;
   p.tileVol = tp.tileVol;
   p.lv = tp.lv;
@@ -179,12 +185,13 @@ cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStr
     p.trSout[t] = tp.trSout[t];
     p.trOut[t] = tp.trOut[t];
   }
-  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(p, ld, st, sm);
+  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(p, ld, st, sm, status);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   dt->ldOff = ld;
   dt->stOff = st;
   dt->stSm = sm;
+  dt->status = status;
   return cudaSuccess;
 }
 
@@ -377,7 +384,7 @@ void tableFree(void* p, cudaStream_t s) {
 cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc, DeviceTables* dt) {
   *alloc = nullptr;
   *dt = DeviceTables();
-  if (pd.kernel != K_TILE || pd.pipe != PIPE_FLAT) return cudaSuccess;
+  if (pd.kernel != K_TILE || !flatTables(pd.pipe)) return cudaSuccess;
   size_t stOffset, smOffset;
   const size_t total = deviceTableBytes(pd.tile, &stOffset, &smOffset);
   void* d = nullptr;

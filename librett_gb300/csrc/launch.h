@@ -13,6 +13,10 @@ struct DeviceTables {
   const int* ldOff = nullptr;
   const int* stOff = nullptr;
   const unsigned short* stSm = nullptr;
+  // Status word after the tables, zero when written; a bulk-copy launch
+  // whose wait for its copies ran out of time sets bit 0 (see
+  // tileKernelBulk) and skips its stores.
+  unsigned* status = nullptr;
 };
 
 // Allocates the plan's tables (from the library's per-device table arena,
@@ -25,8 +29,10 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
 void destroyDeviceTables(void* alloc, cudaStream_t s);
 
 // Device-table layout of a tile: total bytes; ldOff at 0, stOff at
-// *stOffset, stSm at *smOffset (16-byte aligned).
+// *stOffset, stSm at *smOffset (16-byte aligned), then a 16-byte status
+// block.
 size_t deviceTableBytes(const TileParams& tp, size_t* stOffset, size_t* smOffset);
+size_t statusOffset(const TileParams& tp, size_t smOffset);
 
 // Launches a kernel on s that writes the tables of tp at base (which must
 // hold deviceTableBytes), and points *dt at them.

@@ -89,7 +89,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   if (cands.empty()) return LIBRETT_INTERNAL_ERROR;
   int pick = choosePlan(cands, sms, devName, nullptr);
   // Tile problems run the flat pipeline, whose tables go to the scratch.
-  if (cands[pick].kernel == K_TILE && cands[pick].pipe != PIPE_FLAT) {
+  if (cands[pick].kernel == K_TILE && !flatTables(cands[pick].pipe)) {
     int flat = -1;
     for (size_t c = 0; c < cands.size(); ++c)
       if (cands[c].kernel == K_TILE && cands[c].pipe == PIPE_FLAT &&
@@ -103,7 +103,7 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   DeviceTables dt;
   const bool vecOk = ((uintptr_t)idata % 16 == 0 && (uintptr_t)odata % 16 == 0) ||
                      (pd.tile.lv == 1 && pd.tile.sv == 1);
-  if (pd.kernel == K_TILE && pd.pipe == PIPE_FLAT && vecOk) {
+  if (pd.kernel == K_TILE && flatTables(pd.pipe) && vecOk) {
     size_t stOffset, smOffset;
     if (deviceTableBytes(pd.tile, &stOffset, &smOffset) > kScratchBytes)
       return LIBRETT_INVALID_PARAMETER;  // tables exceed the scratch

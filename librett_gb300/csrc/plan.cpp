@@ -269,6 +269,15 @@ GroupRunSplit groupRunSplit(const TileParams& tp) {
   return rs;
 }
 
+int bulkSegment(const TileParams& tp, int padShift) {
+  const int inRun = groupRunSplit(tp).inRun;
+  if (padShift >= PAD_NONE) return inRun;
+  const int block = 1 << padShift;  // elements between two padding gaps
+  if (block % inRun == 0) return inRun;
+  if (inRun % block == 0) return block;
+  return 0;
+}
+
 int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize) {
   long long step = 0;
   int prev = -1;
@@ -515,7 +524,8 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide) {
 // the three pipelines.  Returns false when the tile does not fit the
 // kernels' limits.
 bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp,
-                       bool padSearch = true, long long noneWavefronts = -1) {
+                       bool padSearch = true, long long noneWavefronts = -1,
+                       int bulkMinElems = 0) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
@@ -592,6 +602,8 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
     if (sh < tp.padLog || (!padSearch && sh != PAD_NONE)) continue;
+    // a bulk-copy tile keeps its input segments whole between padding gaps
+    if (bulkMinElems > 0 && sh != PAD_NONE && bulkSegment(tp, sh) < bulkMinElems) continue;
     // the unpadded tile's count may be known from screening
     long long w = sh == PAD_NONE && noneWavefronts >= 0
                       ? noneWavefronts
@@ -613,18 +625,28 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
 
 // Dynamic shared memory of a tile plan for one pipeline.
 int tileSmemBytes(const TileParams& tp, int esize, int pipe) {
-  if (pipe == PIPE_FLAT) return tp.smStride * esize;  // tables live in device memory
+  if (flatTables(pipe)) return tp.smStride * esize;  // tables live in device memory
   const int tableBytes = ((2 * tp.tileVol + 15) / 16) * 16 + ((4 * (tp.nIn + tp.nOut) + 15) / 16) * 16;
   return tableBytes + (pipe == PIPE_ASYNC ? TILE_STAGES : 2) * tp.smStride * esize;
 }
 
+// Smallest bulk copy the bulk pipeline issues: shorter segments move as
+// 16-byte cp.async units in the flat pipeline instead.
+constexpr int BULK_MIN_BYTES = 128;
+
 // PlanDesc of a tile candidate from its geometry and pipeline.
 bool buildTile(const Fused& f, const int64_t* e, int pipe, const TileParams& geom, PlanDesc& pd) {
-  if (pipe == PIPE_ASYNC && geom.lv * f.esize != 16) return false;
+  if ((pipe == PIPE_ASYNC || pipe == PIPE_BULK) && geom.lv * f.esize != 16) return false;
+  int seg = 0;
+  if (pipe == PIPE_BULK) {
+    seg = bulkSegment(geom, geom.padShift);
+    if (seg * f.esize < BULK_MIN_BYTES || geom.tileVol % seg != 0) return false;
+  }
   const int smem = tileSmemBytes(geom, f.esize, pipe);
   if (smem > 227 * 1024) return false;
   pd.pipe = pipe;
   pd.tile = geom;
+  pd.tile.segLen = seg;
   for (int r = 0; r < f.rank; ++r) pd.extent[r] = e[r];
   pd.kernel = K_TILE;
   pd.threads = TILE_THREADS;
@@ -794,7 +816,7 @@ void modelTile(PlanDesc& pd, int numSMs) {
   pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
   // Measured on the random-shape suite: one-tile-per-CTA launches beat the
   // persistent pipelines for most shapes at equal modelled traffic.
-  if (pd.pipe == PIPE_FLAT) pd.cost *= 0.9;
+  if (flatTables(pd.pipe)) pd.cost *= 0.9;
 }
 
 void modelRows(PlanDesc& pd, int numSMs) {
@@ -850,14 +872,24 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
     seen.push_back(key);
     TileParams geom;
     if (!buildTileGeometry(f, e, V, V, geom, !screen)) continue;
-    for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT}) {
+    for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT, PIPE_BULK}) {
       if (pipe != PIPE_FLAT && flatOnly) continue;
       PlanDesc pd;
       pd.f = f;
       pd.targetRunBytes = kb[0];
       pd.maxTileBytes = kb[1];
       pd.screened = geom.screened != 0;
-      if (!buildTile(f, e, pipe, geom, pd)) continue;
+      TileParams g2;
+      const TileParams* use = &geom;
+      if (pipe == PIPE_BULK && !screen && geom.padShift != PAD_NONE &&
+          bulkSegment(geom, geom.padShift) * f.esize < BULK_MIN_BYTES) {
+        // the padding chosen for the other pipelines splits the segments:
+        // search again among the paddings that keep them whole
+        const int bulkMin = (BULK_MIN_BYTES + f.esize - 1) / f.esize;
+        if (!buildTileGeometry(f, e, V, V, g2, true, -1, bulkMin)) continue;
+        use = &g2;
+      }
+      if (!buildTile(f, e, pipe, *use, pd)) continue;
       modelTile(pd, numSMs);
       out.push_back(pd);
     }
@@ -940,8 +972,11 @@ bool refineCandidate(PlanDesc& pd, int numSMs) {
   if (pd.kernel != K_TILE || !pd.screened) return true;
   const int V = 16 / pd.f.esize;
   TileParams geom;
-  // screening simulated the unpadded tile (the same geometry and units)
-  if (!buildTileGeometry(pd.f, pd.extent, V, V, geom, true, pd.tile.bankWavefronts)) return false;
+  // screening simulated the unpadded tile (the same geometry and units);
+  // a bulk-copy tile only takes paddings that keep its segments whole
+  const int bulkMin = pd.pipe == PIPE_BULK ? (BULK_MIN_BYTES + pd.f.esize - 1) / pd.f.esize : 0;
+  if (!buildTileGeometry(pd.f, pd.extent, V, V, geom, true, pd.tile.bankWavefronts, bulkMin))
+    return false;
   PlanDesc full;
   full.f = pd.f;
   full.targetRunBytes = pd.targetRunBytes;

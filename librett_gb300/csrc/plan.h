@@ -25,9 +25,14 @@ constexpr int TILE_STAGES = 3;     // cp.async pipeline depth of the tile kernel
 
 // Tile pipelines: register-staged loads (2 shared buffers) or cp.async
 // straight into a TILE_STAGES-deep ring of shared buffers.
-enum Pipe { PIPE_REG = 0, PIPE_ASYNC = 1, PIPE_FLAT = 2 };
+enum Pipe { PIPE_REG = 0, PIPE_ASYNC = 1, PIPE_FLAT = 2, PIPE_BULK = 3 };
 // PIPE_FLAT: one tile per CTA (no persistent loop); the offset tables are
-// built on the host at plan time and read from device memory.
+// built at plan time and read from device memory.
+// PIPE_BULK: the flat pipeline with its loads as bulk copies: each
+// contiguous segment of the tile's input (an input run, or the part of it
+// between two padding gaps) is one cp.async.bulk into shared memory, all
+// completing on one mbarrier; 16-byte load units only.
+inline bool flatTables(int pipe) { return pipe == PIPE_FLAT || pipe == PIPE_BULK; }
 
 // Transpose methods, numbered as LibreTT's enum (src/plan.h:54-56).
 enum Method { Unknown = 0, Trivial = 1, Packed = 2, PackedSplit = 3, Tiled = 4, TiledCopy = 5 };
@@ -110,6 +115,7 @@ struct TileParams {
   int nRagged;          // grid ranks whose dim is not a multiple of the extent
   int bankWavefronts;   // planner only: simulated wavefronts at padShift
   int screened;         // planner only: built without the padding search
+  int segLen;           // PIPE_BULK: elements per bulk copy (a multiple of lv)
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
@@ -235,6 +241,11 @@ GroupRunSplit groupRunSplit(const TileParams& tp);
 // offset without the table; -1 when the runs are not evenly spaced or
 // s * esize does not fit an int.
 int groupLoadStep(const TileParams& tp, const GroupRunSplit& rs, int esize);
+
+// Elements per bulk copy of a tile in the bulk-copy pipeline at a given
+// padding: the input run when a padding block holds whole runs (or there is
+// no padding), the padding block when a run holds whole blocks, else 0.
+int bulkSegment(const TileParams& tp, int padShift);
 
 // Steps of the store-side run tables where their entries are evenly spaced
 // (the same chain rule over the tile ranks in output order): output run r

@@ -44,7 +44,7 @@ void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   const TileParams& tp = pd.tile;
   out[9] = pd.pipe == PIPE_REG;
   out[10] = pd.pipe == PIPE_ASYNC;
-  out[11] = pd.pipe == PIPE_FLAT;
+  out[11] = flatTables(pd.pipe);
   out[12] = lg2((double)tp.tileVol) / 12.f;
   out[13] = lg2((double)tp.tileVol * f.esize) / 16.f;
   out[19] = pd.slots / 16.f;

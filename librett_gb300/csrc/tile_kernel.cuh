@@ -413,6 +413,114 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
 }
 
+// mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk).
+__device__ __forceinline__ void mbarInit(uint32_t mb, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mb), "r"(count) : "memory");
+}
+
+// Makes an initialised mbarrier visible to the asynchronous proxy (the bulk
+// copies that complete on it).
+__device__ __forceinline__ void mbarInitFence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void mbarArriveExpectTx(uint32_t mb, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbarTryWait(uint32_t mb, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(mb), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// One bulk copy global -> shared (16-byte aligned addresses, size a
+// multiple of 16) that completes `bytes` transactions on mbarrier mb.
+__device__ __forceinline__ void bulkLoad(uint32_t dst, const void* src, uint32_t bytes,
+                                         uint32_t mb) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
+          "r"(dst),
+      "l"(src), "r"(bytes), "r"(mb)
+      : "memory");
+}
+
+__device__ __forceinline__ unsigned long long globalTimerNs() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of mbarrier mb for at most limitNs nanoseconds.
+__device__ __forceinline__ bool mbarWaitBounded(uint32_t mb, uint32_t parity,
+                                                unsigned long long limitNs) {
+  if (mbarTryWait(mb, parity)) return true;
+  const unsigned long long t0 = globalTimerNs();
+  for (;;) {
+    if (mbarTryWait(mb, parity)) return true;
+    if (globalTimerNs() - t0 > limitNs) return false;
+  }
+}
+
+constexpr unsigned long long BULK_WAIT_NS = 1000000000ull;  // 1 s
+
+// Bulk-copy pipeline: the flat kernel with its load phase as bulk copies.
+// The tile's input-order elements form segments of p.segLen elements, each
+// contiguous in global memory (inside one input run) and in shared memory
+// (between two padding gaps); segment k starts at tile element k * segLen,
+// whose global offset is the load-unit table entry of that element.  The
+// CTA's threads issue one cp.async.bulk per segment (no per-unit
+// instruction, no data registers), all completing on one mbarrier that
+// thread 0 arms with the tile's byte count; every thread then waits on it
+// and the stores run as in the flat pipeline.  The wait is bounded: after
+// BULK_WAIT_NS without completion the CTA sets bit 0 of *status, waits once
+// more (bounded) for its copies in flight, and returns without storing.
+template <int ES, int LV, int SV, int NL>
+__global__ void __launch_bounds__(TILE_THREADS)
+tileKernelBulk(const __grid_constant__ TileParams p, const typename Word<ES>::T* __restrict__ in,
+               typename Word<ES>::T* __restrict__ out, const int* __restrict__ ldOff,
+               const int* __restrict__ stOff, const unsigned short* __restrict__ stSm,
+               unsigned* status) {
+  static_assert(ES * LV == 16, "bulk copies need 16-byte load units");
+  using T = typename Word<ES>::T;
+  extern __shared__ __align__(128) unsigned char smraw[];
+  __shared__ __align__(8) unsigned long long bar;
+  T* s = reinterpret_cast<T*>(smraw);
+  long long bin, bout;
+  decodeTile(p, blockIdx.x, bin, bout);
+  const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&bar);
+  const uint32_t sBase = (uint32_t)__cvta_generic_to_shared(s);
+  if (threadIdx.x == 0) {
+    mbarInit(mb, 1);
+    mbarInitFence();
+  }
+  __syncthreads();
+  const int L = p.segLen;
+  const int nSeg = p.tileVol / L;
+  const uint32_t segBytes = (uint32_t)(L * ES);
+  const T* src = in + bin;
+  for (int k = threadIdx.x; k < nSeg; k += TILE_THREADS) {
+    const int j0 = k * L;
+    bulkLoad(sBase + (uint32_t)smemIndex(p, j0) * ES, src + __ldg(ldOff + j0 / LV), segBytes, mb);
+  }
+  if (threadIdx.x == 0) mbarArriveExpectTx(mb, (uint32_t)nSeg * segBytes);
+  constexpr int NS = (NL * LV + SV - 1) / SV;
+  StorePrefetch<SV, NS < 2 ? NS : 2> pf;
+  pf.load(p, stOff, stSm);
+  if (!mbarWaitBounded(mb, 0, BULK_WAIT_NS)) {
+    if (threadIdx.x == 0) atomicOr(status, 1u);
+    mbarWaitBounded(mb, 0, BULK_WAIT_NS);  // copies in flight write this CTA's shared memory
+    return;
+  }
+  storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
+}
+
 // p + i * scale bytes.  With a scale the compiler cannot see (opaque), the
 // offset is one wide integer multiply-add on the FMA pipe instead of a
 // sign extension and a shift-add pair on the ALU pipe, which the grouped

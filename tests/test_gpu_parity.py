@@ -38,6 +38,7 @@ def _run(dims, perm, es, host_bytes, *, candidate=None, measure=False, stream=No
         plan.execute(ip, op)
         torch.cuda.synchronize(dev)
         info = plan.info()
+        info["status"] = plan.status()
     finally:
         plan.destroy()
     res = out.cpu().numpy()
@@ -124,6 +125,36 @@ def test_every_candidate(cuda):
         assert n >= 1
         for c in range(n):
             _check(dims, perm, es, rng=rng, candidate=c)
+
+
+def test_every_candidate_all_pipelines(cuda):
+    """Candidate set 1: the persistent register-staged and cp.async
+    pipelines and the bulk-copy pipeline (one cp.async.bulk per contiguous
+    input segment on an mbarrier) beside the flat one; every candidate
+    bit-exact, and the bulk kernel's status word clear."""
+    lib = L._lib.load()
+    prev = lib.librett_c_set_candidate_set(1)
+    rng = np.random.default_rng(11)
+    probs = [([4, 6, 128, 5, 16], [3, 0, 4, 2, 1], 16), ([300, 7, 11], [1, 2, 0], 8),
+             ([64, 96, 40], [2, 0, 1], 8), ([1024, 512], [1, 0], 4), ([96, 33, 64], [2, 1, 0], 4),
+             ([2, 3, 4, 5, 512, 16], [5, 3, 1, 4, 0, 2], 4), ([48, 40, 3, 20], [3, 2, 0, 1], 16),
+             ([256, 10, 6, 70], [1, 3, 2, 0], 8)]
+    pipes = set()
+    try:
+        for dims, perm, es in probs:
+            n = L.describe(dims, perm, es)["num_candidates"]
+            for c in range(n):
+                info = _check(dims, perm, es, rng=rng, candidate=c)
+                pipes.add(info["pipeline"])
+                assert info["status"] == 0, (dims, perm, es, c)
+            # 16-byte units fall back to element units for unaligned pointers
+            for c in range(n):
+                if L.describe(dims, perm, es, candidate=c)["pipeline"] == 3 and es < 16:
+                    _check(dims, perm, es, rng=rng, candidate=c, offset=es)
+                    break
+    finally:
+        lib.librett_c_set_candidate_set(prev)
+    assert pipes == {0, 1, 2, 3}, pipes
 
 
 @pytest.mark.parametrize("es", [4, 8, 16])
