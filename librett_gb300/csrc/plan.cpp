@@ -554,11 +554,36 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   for (int i = 0; i < f.rank; ++i)
     if (trOfRank[f.perm[i]] >= 0) tp.trOut[k++] = trOfRank[f.perm[i]];
   // Grid ranks, decoded in output order so that consecutive tiles write
-  // neighbouring output.
+  // neighbouring output; except that the first input grid rank goes first
+  // when it has at most kInputFirstChunks chunks (and fewer than the first
+  // output grid rank): then the few tiles that share a band of input run
+  // back to back, and output neighbours are only that many tiles apart, so
+  // both sides' partly shared 64-byte DRAM atoms meet in L2.  On the
+  // random-shape suite this took 17 problems from 0.91-0.95 of their best
+  // to par (up to 14 % faster each), and larger counts measured slower.
+  constexpr int64_t kInputFirstChunks = 16;
+  int order[MAXR];
+  for (int i = 0; i < f.rank; ++i) order[i] = f.perm[i];
+  {
+    int a = -1, b = -1;
+    for (int i = 0; i < f.rank && a < 0; ++i)
+      if (ceilDiv(f.dim[f.perm[i]], e[f.perm[i]]) > 1) a = i;
+    for (int r = 0; r < f.rank && b < 0; ++r)
+      if (ceilDiv(f.dim[r], e[r]) > 1) b = r;
+    if (a >= 0 && b >= 0 && f.perm[a] != b) {
+      const int64_t nb = ceilDiv(f.dim[b], e[b]);
+      if (nb <= kInputFirstChunks && nb < ceilDiv(f.dim[f.perm[a]], e[f.perm[a]])) {
+        int pos = a;
+        while (order[pos] != b) ++pos;
+        for (int i = pos; i > a; --i) order[i] = order[i - 1];
+        order[a] = b;
+      }
+    }
+  }
   int nGR = 0;
   int64_t numTiles = 1;
   for (int i = 0; i < f.rank; ++i) {
-    int r = f.perm[i];
+    int r = order[i];
     int64_t nch = ceilDiv(f.dim[r], e[r]);
     if (nch <= 1) continue;
     if (nch >= (int64_t(1) << 31)) return false;
