@@ -52,10 +52,15 @@ int cachedOccupancy(const void* func, int threads, int smem) {
     if (it != cache.end()) return it->second;
   }
   if (smem > 48 * 1024) {
+    // the opt-in limit covers static and dynamic shared memory together
+    // (the bulk-copy kernel holds its mbarrier in static shared memory)
     int maxOptin = 0;
     cudaDeviceGetAttribute(&maxOptin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (smem > maxOptin) return 0;
-    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, maxOptin) !=
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, func) != cudaSuccess) return 0;
+    const int maxDynamic = maxOptin - (int)fa.sharedSizeBytes;
+    if (smem > maxDynamic) return 0;
+    if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, maxDynamic) !=
         cudaSuccess)
       return 0;
   }

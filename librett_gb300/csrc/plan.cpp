@@ -877,9 +877,10 @@ void modelRows(PlanDesc& pd, int numSMs) {
 }  // namespace
 
 // Tile candidates: (target contiguous run bytes, maximum tile bytes,
-// minimum tile bytes), each in the flat pipeline and, unless flatOnly, the
-// two persistent pipelines.
-void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out,
+// minimum tile bytes), each in every pipeline of the set `pipes` that can run
+// it (bulk copies need 16-byte load units and whole segments of 128 bytes or
+// more).
+void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<PlanDesc>& out,
                           bool screen) {
   const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
                           {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
@@ -897,8 +898,20 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
     seen.push_back(key);
     TileParams geom;
     if (!buildTileGeometry(f, e, V, V, geom, !screen)) continue;
+    int flatIdx = -1;  // this tile's flat candidate in `out`
     for (int pipe : {PIPE_REG, PIPE_ASYNC, PIPE_FLAT, PIPE_BULK}) {
-      if (pipe != PIPE_FLAT && flatOnly) continue;
+      if (!(pipes & (1 << pipe))) continue;
+      if (pipe == PIPE_BULK && flatIdx >= 0 && geom.lv * f.esize == 16) {
+        const int seg = bulkSegment(geom, geom.padShift);
+        if (seg * f.esize >= BULK_MIN_BYTES && geom.tileVol % seg == 0) {
+          // the same tile, geometry and modelled cost as its flat twin
+          PlanDesc pd = out[flatIdx];
+          pd.pipe = PIPE_BULK;
+          pd.tile.segLen = seg;
+          out.push_back(pd);
+          continue;
+        }
+      }
       PlanDesc pd;
       pd.f = f;
       pd.targetRunBytes = kb[0];
@@ -916,6 +929,7 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
       }
       if (!buildTile(f, e, pipe, *use, pd)) continue;
       modelTile(pd, numSMs);
+      if (pipe == PIPE_FLAT) flatIdx = (int)out.size();
       out.push_back(pd);
     }
   }
@@ -924,7 +938,7 @@ void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector
 std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs, bool screen) {
   std::vector<PlanDesc> out;
   out.reserve(12);
-  appendTileCandidates(f, numSMs < 1 ? 1 : numSMs, true, out, screen);
+  appendTileCandidates(f, numSMs < 1 ? 1 : numSMs, PIPES_FLAT, out, screen);
   for (size_t i = 0; i < out.size(); ++i) {
     out[i].candidate = (int)i;
     out[i].numCandidates = (int)out.size();
@@ -984,7 +998,7 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool scree
         out.push_back(pd);
       }
     }
-    appendTileCandidates(f, numSMs, !allPipelines(), out, screen);
+    appendTileCandidates(f, numSMs, allPipelines() ? PIPES_ALL : PIPES_DEFAULT, out, screen);
   }
   for (size_t i = 0; i < out.size(); ++i) {
     out[i].candidate = (int)i;

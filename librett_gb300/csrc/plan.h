@@ -192,9 +192,10 @@ void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
 
 // Candidate plans for a fused problem on a device with numSMs SMs.  The
 // first entry is never empty.  Each candidate's `cost` is filled in.  By
-// default tile candidates use the flat pipeline only (it wins on nearly all
-// measured problems); setAllPipelines(true) or LIBRETT_ALL_PIPELINES=1 adds
-// the persistent register-staged and cp.async variants.
+// default tile candidates use the one-tile-per-CTA pipeline, with per-unit
+// (PIPE_FLAT) and bulk-copy (PIPE_BULK) loads; setAllPipelines(true) or
+// LIBRETT_ALL_PIPELINES=1 adds the persistent register-staged and cp.async
+// variants.
 //
 // screen: build tile candidates without the shared-memory padding search
 // (padding off, bank wavefronts of the unpadded tile), the form the plan
@@ -209,7 +210,16 @@ bool allPipelines();
 // problem (a fused rank-1 copy becomes a one-rank tile); used where every
 // member of a batch must run in that pipeline (grouped execution).
 std::vector<PlanDesc> flatTileCandidates(const Fused& f, int numSMs, bool screen = false);
-void appendTileCandidates(const Fused& f, int numSMs, bool flatOnly, std::vector<PlanDesc>& out,
+
+// Pipelines a tile enumeration builds candidates for (bits 1 << Pipe): the
+// default set is the one-tile-per-CTA pipeline with per-unit and bulk-copy
+// loads; grouped execution uses the first only.
+enum PipeSet {
+  PIPES_FLAT = 1 << PIPE_FLAT,
+  PIPES_DEFAULT = (1 << PIPE_FLAT) | (1 << PIPE_BULK),
+  PIPES_ALL = (1 << PIPE_REG) | (1 << PIPE_ASYNC) | (1 << PIPE_FLAT) | (1 << PIPE_BULK)
+};
+void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<PlanDesc>& out,
                           bool screen = false);
 
 // Index of the candidate the analytic model prefers.

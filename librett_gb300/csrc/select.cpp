@@ -45,6 +45,7 @@ void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   out[9] = pd.pipe == PIPE_REG;
   out[10] = pd.pipe == PIPE_ASYNC;
   out[11] = flatTables(pd.pipe);
+  out[32] = pd.pipe == PIPE_BULK;
   out[12] = lg2((double)tp.tileVol) / 12.f;
   out[13] = lg2((double)tp.tileVol * f.esize) / 16.f;
   out[19] = pd.slots / 16.f;
@@ -190,11 +191,12 @@ inline F4 load4(const float* p) {
 }
 
 // y[r] = relu(b + x[r] . wt) for n rows, wt stored input-major (wt[i][o]).
-// Register-blocked: four rows by 16 outputs accumulate in registers over the
-// inputs (each weight vector loaded once per four rows); each output's sum
+// Register-blocked: RB rows by OB outputs accumulate in registers over the
+// inputs (each weight vector loaded once per RB rows); each output's sum
 // runs in input order starting from the bias.
-void denseRelu(const float* x, int n, int in, const float* wt, const float* b, float* y) {
-  constexpr int RB = 4, OB = 16, NV = OB / 4;
+template <int RB, int OB>
+void denseReluBlocked(const float* x, int n, int in, const float* wt, const float* b, float* y) {
+  constexpr int NV = OB / 4;
   const F4 zero = {0.f, 0.f, 0.f, 0.f};
   for (int r0 = 0; r0 < n; r0 += RB) {
     const float* xr[RB];
@@ -219,6 +221,20 @@ void denseRelu(const float* x, int n, int in, const float* wt, const float* b, f
         }
     }
   }
+}
+
+// Four rows by 16 outputs per block; on AArch64 (32 vector registers), more
+// than four rows go eight at a time by 8 outputs, so each weight vector is
+// loaded once for eight rows (the short list holds up to eight candidates:
+// four tiles with their bulk-copy twins).
+void denseRelu(const float* x, int n, int in, const float* wt, const float* b, float* y) {
+#if defined(__aarch64__)
+  if (n > 4) {
+    denseReluBlocked<8, 8>(x, n, in, wt, b, y);
+    return;
+  }
+#endif
+  denseReluBlocked<4, 16>(x, n, in, wt, b, y);
 }
 
 }  // namespace
@@ -326,11 +342,11 @@ bool loadSelectorModel(const char* path, std::string* why) {
   return true;
 }
 
-// Candidates the learned model ranks: the analytic model's cheapest few.  A
-// short list of 4 (one block of the batched forward) costs no measurable
-// throughput against ranking every candidate (random-shape suite geomean
-// 6399.5 vs 6399.0 GB/s on one GB300, held-out regret 1.53% vs 1.43%), while
-// the network runs on about half of them; 3 cost 0.5% on the suite.
+// Tiles whose candidates the learned model ranks: the analytic model's
+// cheapest few.  A short list of 4 tiles cost no measurable throughput
+// against ranking every candidate (random-shape suite geomean 6399.5 vs
+// 6399.0 GB/s on one GB300, held-out regret 1.53% vs 1.43%), while the
+// network runs on about half of them; 3 cost 0.5% on the suite.
 int shortlistSize() {
   static const int k = [] {
     const char* e = std::getenv("LIBRETT_SELECTOR_SHORTLIST");
@@ -350,12 +366,27 @@ int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* devic
   if (!gLoaded || gModel.sms != numSMs ||
       (deviceName != nullptr && !gModel.device.empty() && gModel.device != deviceName))
     return chooseHeuristic(cands);
-  // the short list: candidates in increasing analytic cost (ties by index)
+  // the short list: the candidates of the analytic model's cheapest few
+  // tiles, in increasing analytic cost (ties by index); a tile's per-unit
+  // and bulk-copy variants (same extents, same modelled cost) count once
   std::vector<int> order(cands.size());
   for (size_t c = 0; c < order.size(); ++c) order[c] = (int)c;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return cands[a].cost < cands[b].cost; });
-  const int n = std::min((int)order.size(), shortlistSize());
+  auto sameTile = [&](int a, int b) {
+    const PlanDesc& x = cands[a];
+    const PlanDesc& y = cands[b];
+    if (x.kernel != K_TILE || y.kernel != K_TILE) return false;
+    for (int r = 0; r < x.f.rank; ++r)
+      if (x.extent[r] != y.extent[r]) return false;
+    return true;
+  };
+  int n = 0;
+  for (int tiles = 0; n < (int)order.size(); ++n) {
+    bool twin = false;
+    for (int j = 0; j < n && !twin; ++j) twin = sameTile(order[j], order[n]);
+    if (!twin && tiles++ == shortlistSize()) break;
+  }
   if (n == 1) return order[0];
   std::vector<float> x((size_t)n * NFEAT), y(n);
   for (int c = 0; c < n; ++c) {

@@ -14,7 +14,7 @@
 
 namespace lt {
 
-constexpr int NFEAT = 32;      // features per candidate
+constexpr int NFEAT = 33;      // features per candidate
 constexpr int MLP_HIDDEN = 128;
 constexpr int MLP_LAYERS = 4;  // 3 hidden layers + output
 

@@ -18,6 +18,10 @@ Both datasets from the committed timings (host only; writes data.npz and
 data_large.npz):
     python -m librett_gb300.learn.data \
         --from-timings librett_gb300/models/plan_timings_gb300.npz --out data.npz
+Packing two collected datasets (base distribution, large-problem
+supplement) into a timing file of that form (host only):
+    python -m librett_gb300.learn.data --pack data.npz data_large.npz \
+        --out librett_gb300/models/plan_timings_gb300.npz
 """
 from __future__ import annotations
 
@@ -156,6 +160,15 @@ def from_timings(path):
     return refeature(base), refeature(large)
 
 
+def pack_timings(base, large):
+    """The committed timing-file form of two collected datasets: problems,
+    candidate indices and times only (features are recomputed on load)."""
+    return {"problems": base["problems"], "prob": base["prob"], "cand": base["cand"],
+            "t": base["t"], "large_problems": large["problems"], "large_prob": large["prob"],
+            "large_cand": large["cand"], "large_t": large["t"], "sms": base["sms"],
+            "device": base["device"]}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
     ap.add_argument("--problems", type=int, default=6000)
@@ -167,7 +180,15 @@ def main(argv=None):
                     help="recompute features of this dataset (no GPU needed) instead of timing")
     ap.add_argument("--from-timings", default=None,
                     help="build both datasets from a committed timing file (no GPU needed)")
+    ap.add_argument("--pack", nargs=2, default=None, metavar=("BASE", "LARGE"),
+                    help="write the timing file of two collected datasets (no GPU needed)")
     args = ap.parse_args(argv)
+    if args.pack:
+        zb, zl = np.load(args.pack[0]), np.load(args.pack[1])
+        out = pack_timings({k: zb[k] for k in zb.files}, {k: zl[k] for k in zl.files})
+        np.savez_compressed(args.out, **out)
+        print(f"wrote {args.out}: {len(out['t'])} + {len(out['large_t'])} timings")
+        return 0
     if args.refeature:
         z = np.load(args.refeature)
         data = refeature({k: z[k] for k in z.files})

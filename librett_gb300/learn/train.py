@@ -215,14 +215,17 @@ def geo_regret(reg):
 
 # Feature columns (librett_gb300/csrc/select.cpp planFeatures): 9 and 10 mark
 # the persistent pipelines, which are not in the default candidate set; 30 is
-# the analytic model's cost (log scale, monotone in it).
-PIPE_REG_COL, PIPE_ASYNC_COL, COST_COL = 9, 10, 30
+# the analytic model's cost (log scale, monotone in it); 32 marks a bulk-copy
+# variant, which shares its tile (and the columns below) with a per-unit one.
+PIPE_REG_COL, PIPE_ASYNC_COL, COST_COL, BULK_COL = 9, 10, 30, 32
+TILE_COLS = [8, 12, 13, 14, 15, 16, 17, 18, 30]
 
 
 def shortlist_regret(score, X, t, prob, k):
     """Regret of the deployed selection, per problem: within the default
-    candidate set, the lowest score among the analytic model's k cheapest
-    candidates (k <= 0: among all), against the set's measured best."""
+    candidate set, the lowest score among the candidates of the analytic
+    model's k cheapest tiles (a tile's per-unit and bulk-copy variants count
+    once; k <= 0: among all), against the set's measured best."""
     default = (X[:, PIPE_REG_COL] == 0) & (X[:, PIPE_ASYNC_COL] == 0)
     reg = []
     for p in np.unique(prob):
@@ -231,7 +234,15 @@ def shortlist_regret(score, X, t, prob, k):
             continue
         keep = m[np.argsort(X[m, COST_COL], kind="stable")]
         if k > 0:
-            keep = keep[:k]
+            tiles, n = [], 0
+            for i in keep:
+                key = tuple(X[i, TILE_COLS])
+                if key not in tiles:
+                    if len(tiles) == k:
+                        break
+                    tiles.append(key)
+                n += 1
+            keep = keep[:n]
         pick = keep[np.argmin(score[keep])]
         reg.append(t[pick] / t[m].min() - 1.0)
     return np.array(reg)
@@ -246,7 +257,7 @@ def evaluate_model(d, model, holdout):
     rep = {}
     for name, mask in (("train", prob < split), ("holdout", prob >= split)):
         r = {}
-        for k in (0, 4, 3):
+        for k in (0, 4, 3, 2):
             reg = shortlist_regret(pred[mask], X[mask], t[mask], prob[mask], k)
             r[f"shortlist_{k or 'all'}"] = {"geomean_regret": geo_regret(reg),
                                              "p90_regret": float(np.quantile(reg, 0.9)),

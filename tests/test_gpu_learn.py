@@ -3,11 +3,12 @@ float64 oracle, and a short training run."""
 import numpy as np
 import pytest
 
+from librett_gb300 import _lib
 from librett_gb300.learn import train as T
 from oracle import mlp_oracle as M
 
 pytestmark = pytest.mark.gpu
-NF = 32
+NF = _lib.load().librett_c_mlp_feature_count()
 
 
 def test_gradients_match_float64_oracle(cuda):

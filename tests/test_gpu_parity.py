@@ -119,12 +119,18 @@ def test_every_candidate(cuda):
              ([2, 3, 4, 5, 512, 16], [5, 3, 1, 4, 0, 2], 4), ([300, 7, 11], [0, 2, 1], 8),
              ([33, 65, 17], [1, 2, 0], 8), ([1024, 1024], [1, 0], 4),
              # element loads with 16-byte stores and an odd unit count
-             ([51, 2, 1354, 2, 9], [1, 3, 0, 2, 4], 4)]
+             ([51, 2, 1354, 2, 9], [1, 3, 0, 2, 4], 4),
+             # bulk-copy tiles above 48 KB of shared memory (opt-in limit)
+             ([128, 64, 6], [1, 0, 2], 16), ([96, 100, 24], [1, 0, 2], 16)]
+    big_bulk = 0
     for dims, perm, es in probs:
         n = L.describe(dims, perm, es)["num_candidates"]
         assert n >= 1
         for c in range(n):
-            _check(dims, perm, es, rng=rng, candidate=c)
+            info = _check(dims, perm, es, rng=rng, candidate=c)
+            assert info["status"] == 0
+            big_bulk += info["pipeline"] == 3 and info["smem_bytes"] > 48 * 1024
+    assert big_bulk >= 2
 
 
 def test_every_candidate_all_pipelines(cuda):

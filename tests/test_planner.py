@@ -51,7 +51,7 @@ def _check_plan(dims, perm, es, candidate=-1):
     assert info["slots"] in (1, 2, 4, 8, 16)
     assert info["num_tiles"] == int(np.prod([-(-d // e) for d, e in zip(fd, ext)]))
     assert info["smem_bytes"] <= 227 * 1024
-    buffers = 1 if info["pipeline"] == 2 else 2
+    buffers = 1 if info["pipeline"] in (2, 3) else 2  # one-tile-per-CTA pipelines: one buffer
     assert info["smem_bytes"] >= buffers * tvol * es
     ragged = sum(1 for d, e in zip(fd, ext) if d % e)
     assert ragged <= 2

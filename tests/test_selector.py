@@ -13,7 +13,7 @@ from librett_gb300.learn import data as D
 from librett_gb300.learn import train as T
 from oracle import mlp_oracle as M
 
-NF = 32
+NF = _lib.load().librett_c_mlp_feature_count()
 
 
 @pytest.fixture
@@ -114,8 +114,9 @@ def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selec
 
 
 def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore_selector):
-    """The analytic model short-lists its 4 cheapest candidates (ties by
-    index); the learned pick is the lowest prediction among those."""
+    """The analytic model short-lists the candidates of its 4 cheapest tiles
+    (ties by index; a tile's per-unit and bulk-copy variants count once);
+    the learned pick is the lowest prediction among those."""
     lib = restore_selector
     path, params = _write(tmp_path, sms=152)
     assert lib.librett_c_load_plan_model(path.encode()) == 0
@@ -124,8 +125,17 @@ def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore
         n = L.describe(dims, perm, es)["num_candidates"]
         X = np.stack([D.features(dims, perm, es, c) for c in range(n)])
         pred, _ = M.forward(params, X)
-        cost = [L.describe(dims, perm, es, candidate=c)["model_cost"] for c in range(n)]
-        short = sorted(range(n), key=lambda c: cost[c])[:4]
+        infos = [L.describe(dims, perm, es, candidate=c) for c in range(n)]
+        order = sorted(range(n), key=lambda c: infos[c]["model_cost"])
+        key = [tuple(i["tile_extent"]) if i["method"] in (2, 3, 4) else ("kernel", c)
+               for c, i in enumerate(infos)]
+        tiles, short = [], []
+        for c in order:
+            if key[c] not in tiles:
+                if len(tiles) == 4:
+                    break
+                tiles.append(key[c])
+            short.append(c)
         got = L.describe(dims, perm, es)["candidate"]
         assert got in short
         best = pred[short].min()
@@ -138,6 +148,7 @@ def test_shortlist_regret_rules():
     the lowest score on it, regret against the set's best."""
     X = np.zeros((5, NF), dtype=np.float32)
     X[:, T.COST_COL] = [0.1, 0.2, 0.3, 0.4, 0.0]
+    X[:, 12] = [1, 2, 3, 4, 5]  # five different tiles
     X[4, T.PIPE_REG_COL] = 1  # cheapest and fastest, but not a default candidate
     t = np.array([3.0, 2.0, 1.5, 1.0, 0.5])
     prob = np.zeros(5, dtype=int)
@@ -145,6 +156,13 @@ def test_shortlist_regret_rules():
     assert T.shortlist_regret(score, X, t, prob, 0)[0] == 0.0  # picks candidate 3
     assert T.shortlist_regret(score, X, t, prob, 3)[0] == 0.5  # 2 of {0, 1, 2}: 1.5 / 1.0
     assert T.shortlist_regret(score, X, t, prob, 1)[0] == 2.0  # only 0: 3.0 / 1.0
+    # a bulk-copy twin of tile 0 (same tile columns) joins the short list of 1
+    X2 = np.concatenate([X, X[:1]])
+    X2[5, T.BULK_COL] = 1
+    t2 = np.concatenate([t, [1.2]])
+    score2 = np.concatenate([score, [4.5]])
+    prob2 = np.zeros(6, dtype=int)
+    assert abs(T.shortlist_regret(score2, X2, t2, prob2, 1)[0] - 0.2) < 1e-12
 
 
 def test_targets_relative_and_clipped():
