@@ -919,7 +919,8 @@ def run_engine(args):
         plans = []
         del inp, out
         torch.cuda.empty_cache()
-        configs = extra_legs(args, dev, stream, peak)
+        suite_gbs = [2 * problem_bytes(p) / (t / 1e3) / 1e9 for p, t in zip(problems, per_problem_ms)]
+        configs = extra_legs(args, dev, stream, peak, suite_gbs)
 
     if rank != 0:
         return 0
@@ -968,7 +969,7 @@ def run_engine(args):
     return 0
 
 
-def extra_legs(args, dev, stream, peak):
+def extra_legs(args, dev, stream, peak, suite_gbs=None):
     """C1, C3a, C3b, the grouped batch, planning latency and plan-choice
     regret, each measured in this run, plus LibreTT's CUDA build on C1, C3a,
     C3b and the first suite problems when it is present."""
@@ -992,6 +993,12 @@ def extra_legs(args, dev, stream, peak):
             if r.get("gbs_plan"):
                 out[name]["vs_librett_plan"] = round(mine / r["gbs_plan"], 3)
                 out[name]["vs_librett_plan_measure"] = round(mine / r["gbs_plan_measure"], 3)
+        if suite_gbs is not None and len(suite_gbs) >= LIBRETT_SUITE and "suite40" in ref:
+            mine = float(np.exp(np.mean(np.log(suite_gbs[:LIBRETT_SUITE]))))
+            ref["suite40"]["engine_geomean_gbs"] = round(mine, 1)
+            ref["suite40"]["vs_librett_plan"] = round(mine / ref["suite40"]["geomean_gbs_plan"], 3)
+            ref["suite40"]["vs_librett_plan_measure"] = round(
+                mine / ref["suite40"]["geomean_gbs_plan_measure"], 3)
         lat = ref.get("planning_us_median", {})
         if lat.get("librettPlanMeasure"):
             out["planning"]["vs_librett_plan_measure"] = round(
