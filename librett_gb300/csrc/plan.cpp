@@ -905,10 +905,9 @@ void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<Pla
         const int seg = bulkSegment(geom, geom.padShift);
         if (seg * f.esize >= BULK_MIN_BYTES && geom.tileVol % seg == 0) {
           // the same tile, geometry and modelled cost as its flat twin
-          PlanDesc pd = out[flatIdx];
-          pd.pipe = PIPE_BULK;
-          pd.tile.segLen = seg;
-          out.push_back(pd);
+          out.push_back(out[flatIdx]);
+          out.back().pipe = PIPE_BULK;
+          out.back().tile.segLen = seg;
           continue;
         }
       }
@@ -964,7 +963,7 @@ bool allPipelines() {
 
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool screen) {
   std::vector<PlanDesc> out;
-  out.reserve(allPipelines() ? 32 : 12);
+  out.reserve(allPipelines() ? 40 : 24);  // candidates are ~4 KB: no regrowth
   if (numSMs < 1) numSMs = 1;
   if (f.rank == 1) {
     PlanDesc pd;
