@@ -91,6 +91,18 @@ int librett_c_plan_info(librettHandle handle, librett_plan_info* info);
  * counterpart (LibreTT exits on device errors, src/GpuUtils.h:47-56). */
 int librett_c_plan_status(librettHandle handle, unsigned* status);
 
+/* Test hook for the bulk-copy pipeline's bounded wait (no LibreTT
+ * counterpart): launches the plan (which must be a bulk-copy plan, pointers
+ * 16-byte aligned) once with `extra_bytes` (1..4096) more transaction bytes
+ * armed on each CTA's mbarrier than its copies deliver, so that no wait can
+ * complete: every CTA gives up after its time limit (about 1 s, then up to
+ * 1 s more for its copies), sets the status bit and skips its stores.
+ * Synchronises the plan's stream, returns the status word the launch left in
+ * *status (1 expected) and clears it; the plan stays usable.  Nothing faults:
+ * the copies complete, only the armed count is never reached. */
+int librett_c_bulk_wait_test(librettHandle handle, const void* idata, void* odata,
+                             unsigned extra_bytes, unsigned* status);
+
 /* Host-only planning without a device or a handle: runs the same input check,
  * rank fusion and tile choice as librett_c_plan for a device with `num_sms`
  * SMs.  candidate < 0 picks the planner's default; otherwise the numbered

@@ -151,6 +151,8 @@ C_FUNCTIONS = [
       ctypes.POINTER(ctypes.c_longlong)]),
     ("librett_c_inject_fault", ctypes.c_int, [ctypes.c_int, ctypes.c_longlong]),
     ("librett_c_plan_status", ctypes.c_int, [_H, ctypes.POINTER(ctypes.c_uint)]),
+    ("librett_c_bulk_wait_test", ctypes.c_int,
+     [_H, _P, _P, ctypes.c_uint, ctypes.POINTER(ctypes.c_uint)]),
     ("librett_c_result_string", ctypes.c_char_p, [ctypes.c_int]),
 ]
 

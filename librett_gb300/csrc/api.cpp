@@ -622,3 +622,25 @@ int librett_c_plan_status(librettHandle handle, unsigned* status) {
     return LIBRETT_INTERNAL_ERROR;
   return LIBRETT_SUCCESS;
 }
+
+int librett_c_bulk_wait_test(librettHandle handle, const void* idata, void* odata,
+                             unsigned extra_bytes, unsigned* status) {
+  if (status == nullptr || extra_bytes == 0 || extra_bytes > 4096) return LIBRETT_INVALID_PARAMETER;
+  std::shared_ptr<PlanObj> obj = lt::findPlan(handle);
+  if (!obj) return LIBRETT_INVALID_PLAN;
+  if (obj->pd.kernel != lt::K_TILE || obj->pd.pipe != lt::PIPE_BULK ||
+      obj->tables.status == nullptr || obj->needsScalar(idata, odata))
+    return LIBRETT_INVALID_PARAMETER;
+  lt::PlanDesc pd = obj->pd;
+  pd.tile.testExtraTx = (int)extra_bytes;
+  int grid = 0;
+  *status = 0;
+  if (lt::launchPlan(pd, &obj->tables, idata, odata, obj->stream, obj->numSMs, &grid) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(status, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                      obj->stream) != cudaSuccess ||
+      cudaMemsetAsync(obj->tables.status, 0, sizeof(unsigned), obj->stream) != cudaSuccess ||
+      cudaStreamSynchronize(obj->stream) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
+  return LIBRETT_SUCCESS;
+}

@@ -419,11 +419,11 @@ long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
   return cost;
 }
 
-// Input-order index of the first sampleUnits store units' elements
-// (element m of unit w at [m * n + w]); independent of the padding.
-std::vector<int> storeSample(const TileParams& tp, int sampleUnits, int& n) {
-  n = std::min(tp.nOut, sampleUnits);
-  std::vector<int> j((size_t)n * tp.sv);
+// Input-order index of the first n = min(nOut, sampleUnits) store units'
+// elements (element m of unit w at j[m * n + w], n * sv entries); independent
+// of the padding.  Returns n.
+int storeSample(const TileParams& tp, int sampleUnits, int* j) {
+  const int n = std::min(tp.nOut, sampleUnits);
   // output-order elements q = w * sv + m in sequence: a mixed-radix counter
   // over the tile ranks in output order carries the input-order index
   int digit[MAXR] = {};
@@ -439,11 +439,11 @@ std::vector<int> storeSample(const TileParams& tp, int sampleUnits, int& n) {
         digit[i] = 0;
       }
     }
-  return j;
+  return n;
 }
 
 long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits,
-                     const std::vector<int>& jStore, int nStore) {
+                     const int* jStore, int nStore) {
   const int words = esize / 4;
   auto smIdx = [&](int j) { return j + ((j >> padShift) << tp.padLog); };
   int addr[32];
@@ -474,9 +474,9 @@ long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUn
 }  // namespace
 
 long long smemWavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits) {
-  int n = 0;
-  const std::vector<int> j = storeSample(tp, sampleUnits, n);
-  return wavefronts(tp, esize, padShift, sampleUnits, j, n);
+  std::vector<int> j((size_t)std::min(tp.nOut, std::max(sampleUnits, 0)) * tp.sv);
+  const int n = storeSample(tp, sampleUnits, j.data());
+  return wavefronts(tp, esize, padShift, sampleUnits, j.data(), n);
 }
 
 namespace {
@@ -622,8 +622,8 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
     if (worst > 65535 || tableBytes + TILE_STAGES * worst * f.esize > 227 * 1024) padSearch = true;
   }
   tp.screened = padSearch ? 0 : 1;
-  int nStore = 0;
-  const std::vector<int> jStore = storeSample(tp, 64, nStore);
+  int jStore[64 * 4];  // 64 store units of at most 4 elements
+  const int nStore = storeSample(tp, 64, jStore);
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
     if (sh < tp.padLog || (!padSearch && sh != PAD_NONE)) continue;
@@ -885,17 +885,21 @@ void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<Pla
   const int knobs[][3] = {{512, 16384, 8192},  {256, 8192, 4096},   {128, 4096, 2048},
                           {1024, 32768, 16384}, {512, 32768, 16384}, {256, 4096, 0},
                           {2048, 65536, 32768}, {64, 2048, 0},       {256, 16384, 16384}};
-  std::vector<std::vector<int64_t>> seen;
+  constexpr int NKNOBS = sizeof(knobs) / sizeof(knobs[0]);
+  int64_t seen[NKNOBS][MAXR];  // extents already enumerated
+  int nSeen = 0;
   const int V = 16 / f.esize;
   for (auto& kb : knobs) {
     int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
     int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
     int64_t fillVol = std::min<int64_t>(maxVol, kb[2] / f.esize);
-    int64_t e[MAXR];
+    int64_t* e = seen[nSeen];
     chooseExtents(f, target, maxVol, fillVol, e);
-    std::vector<int64_t> key(e, e + f.rank);
-    if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
-    seen.push_back(key);
+    bool dup = false;
+    for (int k = 0; k < nSeen && !dup; ++k)
+      dup = std::equal(e, e + f.rank, seen[k]);
+    if (dup) continue;
+    ++nSeen;
     TileParams geom;
     if (!buildTileGeometry(f, e, V, V, geom, !screen)) continue;
     int flatIdx = -1;  // this tile's flat candidate in `out`
@@ -911,7 +915,8 @@ void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<Pla
           continue;
         }
       }
-      PlanDesc pd;
+      out.emplace_back();  // built in place (a candidate is ~4 KB)
+      PlanDesc& pd = out.back();
       pd.f = f;
       pd.targetRunBytes = kb[0];
       pd.maxTileBytes = kb[1];
@@ -923,13 +928,18 @@ void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<Pla
         // the padding chosen for the other pipelines splits the segments:
         // search again among the paddings that keep them whole
         const int bulkMin = (BULK_MIN_BYTES + f.esize - 1) / f.esize;
-        if (!buildTileGeometry(f, e, V, V, g2, true, -1, bulkMin)) continue;
+        if (!buildTileGeometry(f, e, V, V, g2, true, -1, bulkMin)) {
+          out.pop_back();
+          continue;
+        }
         use = &g2;
       }
-      if (!buildTile(f, e, pipe, *use, pd)) continue;
+      if (!buildTile(f, e, pipe, *use, pd)) {
+        out.pop_back();
+        continue;
+      }
       modelTile(pd, numSMs);
-      if (pipe == PIPE_FLAT) flatIdx = (int)out.size();
-      out.push_back(pd);
+      if (pipe == PIPE_FLAT) flatIdx = (int)out.size() - 1;
     }
   }
 }

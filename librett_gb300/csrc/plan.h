@@ -116,6 +116,8 @@ struct TileParams {
   int bankWavefronts;   // planner only: simulated wavefronts at padShift
   int screened;         // planner only: built without the padding search
   int segLen;           // PIPE_BULK: elements per bulk copy (a multiple of lv)
+  int testExtraTx;      // PIPE_BULK, test hook only: bytes armed on the mbarrier beyond
+                        // the tile's (0; nonzero makes the bounded wait run out)
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)

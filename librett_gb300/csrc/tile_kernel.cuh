@@ -509,7 +509,7 @@ tileKernelBulk(const __grid_constant__ TileParams p, const typename Word<ES>::T*
     const int j0 = k * L;
     bulkLoad(sBase + (uint32_t)smemIndex(p, j0) * ES, src + __ldg(ldOff + j0 / LV), segBytes, mb);
   }
-  if (threadIdx.x == 0) mbarArriveExpectTx(mb, (uint32_t)nSeg * segBytes);
+  if (threadIdx.x == 0) mbarArriveExpectTx(mb, (uint32_t)nSeg * segBytes + (uint32_t)p.testExtraTx);
   constexpr int NS = (NL * LV + SV - 1) / SV;
   StorePrefetch<SV, NS < 2 ? NS : 2> pf;
   pf.load(p, stOff, stSm);

@@ -221,11 +221,15 @@ PIPE_REG_COL, PIPE_ASYNC_COL, COST_COL, BULK_COL = 9, 10, 30, 32
 TILE_COLS = [8, 12, 13, 14, 15, 16, 17, 18, 30]
 
 
-def shortlist_regret(score, X, t, prob, k):
+SHORTLIST_TWINS = 2  # short-listed tiles that keep their bulk-copy twin
+
+
+def shortlist_regret(score, X, t, prob, k, twins=SHORTLIST_TWINS):
     """Regret of the deployed selection, per problem: within the default
     candidate set, the lowest score among the candidates of the analytic
     model's k cheapest tiles (a tile's per-unit and bulk-copy variants count
-    once; k <= 0: among all), against the set's measured best."""
+    once, and only the `twins` cheapest tiles keep the bulk-copy variant;
+    k <= 0: among all), against the set's measured best."""
     default = (X[:, PIPE_REG_COL] == 0) & (X[:, PIPE_ASYNC_COL] == 0)
     reg = []
     for p in np.unique(prob):
@@ -234,15 +238,17 @@ def shortlist_regret(score, X, t, prob, k):
             continue
         keep = m[np.argsort(X[m, COST_COL], kind="stable")]
         if k > 0:
-            tiles, n = [], 0
+            tiles, short = [], []
             for i in keep:
                 key = tuple(X[i, TILE_COLS])
                 if key not in tiles:
                     if len(tiles) == k:
                         break
                     tiles.append(key)
-                n += 1
-            keep = keep[:n]
+                if X[i, BULK_COL] == 1 and tiles.index(key) >= twins:
+                    continue
+                short.append(i)
+            keep = np.array(short, dtype=keep.dtype)
         pick = keep[np.argmin(score[keep])]
         reg.append(t[pick] / t[m].min() - 1.0)
     return np.array(reg)

@@ -6,7 +6,15 @@ failures here are made on the host (librett_c_inject_fault reports a CUDA
 error before the device is called), so no GPU ever faults: each test arms one
 site, checks the error code, then checks that the next call through the same
 path succeeds and transposes correctly.
+
+The bulk-copy pipeline's bounded mbarrier wait is driven the same way: a
+test launch arms more bytes than the copies deliver (a count nothing
+completes), so the wait runs out and the kernel reports it in the plan's
+status word; the copies themselves land normally.
 """
+import ctypes
+import time
+
 import numpy as np
 import pytest
 
@@ -135,3 +143,62 @@ def test_noalloc_launch_failure(cuda, disarm):
                                out.data_ptr()) == L.LIBRETT_SUCCESS
     torch.cuda.synchronize()
     assert np.array_equal(out.cpu().numpy(), O.transpose_np(host, DIMS, PERM, ES).view(np.uint8))
+
+
+def _bulk_candidate(dims, perm, es):
+    n = L.describe(dims, perm, es)["num_candidates"]
+    for c in range(n):
+        info = L.describe(dims, perm, es, candidate=c)
+        if info["pipeline"] == 3 and info["num_tiles"] <= 4:
+            return c, info
+    raise AssertionError("no bulk-copy candidate with at most 4 tiles")
+
+
+def test_bulk_wait_test_arguments():
+    lib = _lib.load()
+    st = ctypes.c_uint(0)
+    assert lib.librett_c_bulk_wait_test(0, None, None, 16, ctypes.byref(st)) != L.LIBRETT_SUCCESS
+    assert lib.librett_c_bulk_wait_test(0, None, None, 16, None) == L.LIBRETT_INVALID_PARAMETER
+
+
+@pytest.mark.gpu
+def test_bulk_wait_runs_out_and_reports(cuda):
+    """Each CTA of a bulk-copy launch whose mbarrier never completes gives up
+    after its time limit (about 1 s, then at most 1 s more for its copies),
+    sets status bit 0 and stores nothing; the plan's status reads 0 again
+    afterwards and its next execute is correct."""
+    import torch
+
+    dims, perm, es = [64, 32], [1, 0], 8
+    cand, info = _bulk_candidate(dims, perm, es)
+    host, inp = _data(dims, es)
+    out = torch.full_like(inp, 0xA5)
+    s = torch.cuda.current_stream()
+    lib = _lib.load()
+    want = O.transpose_np(host, dims, perm, es).view(np.uint8)
+    with L.Plan(dims, perm, es, s, candidate=cand) as p:
+        assert p.info()["pipeline"] == 3
+        # wrong plan kind or arguments are refused before any launch
+        st = ctypes.c_uint(7)
+        for extra in (0, 4097):
+            assert lib.librett_c_bulk_wait_test(p.handle, inp.data_ptr(), out.data_ptr(), extra,
+                                                ctypes.byref(st)) == L.LIBRETT_INVALID_PARAMETER
+        assert lib.librett_c_bulk_wait_test(p.handle, inp.data_ptr() + 8, out.data_ptr(), 16,
+                                            ctypes.byref(st)) == L.LIBRETT_INVALID_PARAMETER
+        torch.cuda.synchronize()
+        t0 = time.monotonic()
+        rc = lib.librett_c_bulk_wait_test(p.handle, inp.data_ptr(), out.data_ptr(), 16,
+                                          ctypes.byref(st))
+        waited = time.monotonic() - t0
+        assert rc == L.LIBRETT_SUCCESS and st.value == 1
+        assert 0.9 < waited < 30.0, waited
+        assert bool((out == 0xA5).all())  # no CTA stored
+        assert p.status() == 0
+        p.execute(inp.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        assert p.status() == 0
+    assert np.array_equal(out.cpu().numpy(), want)
+    with L.Plan(dims, perm, es, s) as p:  # a plan that is not bulk-copy is refused
+        if p.info()["pipeline"] != 3:
+            assert lib.librett_c_bulk_wait_test(p.handle, inp.data_ptr(), out.data_ptr(), 16,
+                                                ctypes.byref(st)) == L.LIBRETT_INVALID_PARAMETER

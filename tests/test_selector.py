@@ -115,8 +115,9 @@ def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selec
 
 def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore_selector):
     """The analytic model short-lists the candidates of its 4 cheapest tiles
-    (ties by index; a tile's per-unit and bulk-copy variants count once);
-    the learned pick is the lowest prediction among those."""
+    (ties by index; a tile's per-unit and bulk-copy variants count once, and
+    only the 2 cheapest tiles keep the bulk-copy variant); the learned pick
+    is the lowest prediction among those."""
     lib = restore_selector
     path, params = _write(tmp_path, sms=152)
     assert lib.librett_c_load_plan_model(path.encode()) == 0
@@ -135,6 +136,8 @@ def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore
                 if len(tiles) == 4:
                     break
                 tiles.append(key[c])
+            if infos[c]["pipeline"] == 3 and tiles.index(key[c]) >= T.SHORTLIST_TWINS:
+                continue
             short.append(c)
         got = L.describe(dims, perm, es)["candidate"]
         assert got in short
@@ -163,6 +166,13 @@ def test_shortlist_regret_rules():
     score2 = np.concatenate([score, [4.5]])
     prob2 = np.zeros(6, dtype=int)
     assert abs(T.shortlist_regret(score2, X2, t2, prob2, 1)[0] - 0.2) < 1e-12
+    # a twin of the third-cheapest tile stays off the short list
+    X3 = np.concatenate([X, X[2:3]])
+    X3[5, T.BULK_COL] = 1
+    t3 = np.concatenate([t, [0.6]])
+    score3 = np.concatenate([score, [-5.0]])
+    assert T.shortlist_regret(score3, X3, t3, prob2, 3)[0] == 1.5 / 0.6 - 1.0  # picks 2
+    assert T.shortlist_regret(score3, X3, t3, prob2, 3, twins=3)[0] == 0.0
 
 
 def test_targets_relative_and_clipped():
