@@ -365,8 +365,9 @@ int shortlistSize() {
 // Of the short-listed tiles, the cheapest SHORTLIST_TWINS also bring their
 // bulk-copy twin.  Held out (1,000 problems): twins of all 4 tiles 2.02 %
 // regret over 6.2 candidates, of the first 2 tiles 2.14 % over 5.0, of
-// none 2.66 % over 3.7.
-constexpr int SHORTLIST_TWINS = 2;
+// none 2.66 % over 3.7; on the random-shape suite (1 GiB problems) twins of
+// only 2 tiles cost 0.4 % of throughput on one GB300, so all 4 keep them.
+constexpr int SHORTLIST_TWINS = 4;
 
 int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
                bool* usedLearned) {

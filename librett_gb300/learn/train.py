@@ -221,7 +221,7 @@ PIPE_REG_COL, PIPE_ASYNC_COL, COST_COL, BULK_COL = 9, 10, 30, 32
 TILE_COLS = [8, 12, 13, 14, 15, 16, 17, 18, 30]
 
 
-SHORTLIST_TWINS = 2  # short-listed tiles that keep their bulk-copy twin
+SHORTLIST_TWINS = 4  # short-listed tiles that keep their bulk-copy twin
 
 
 def shortlist_regret(score, X, t, prob, k, twins=SHORTLIST_TWINS):

@@ -116,8 +116,8 @@ def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selec
 def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore_selector):
     """The analytic model short-lists the candidates of its 4 cheapest tiles
     (ties by index; a tile's per-unit and bulk-copy variants count once, and
-    only the 2 cheapest tiles keep the bulk-copy variant); the learned pick
-    is the lowest prediction among those."""
+    only the SHORTLIST_TWINS cheapest tiles keep the bulk-copy variant); the
+    learned pick is the lowest prediction among those."""
     lib = restore_selector
     path, params = _write(tmp_path, sms=152)
     assert lib.librett_c_load_plan_model(path.encode()) == 0
@@ -171,7 +171,7 @@ def test_shortlist_regret_rules():
     X3[5, T.BULK_COL] = 1
     t3 = np.concatenate([t, [0.6]])
     score3 = np.concatenate([score, [-5.0]])
-    assert T.shortlist_regret(score3, X3, t3, prob2, 3)[0] == 1.5 / 0.6 - 1.0  # picks 2
+    assert T.shortlist_regret(score3, X3, t3, prob2, 3, twins=2)[0] == 1.5 / 0.6 - 1.0  # picks 2
     assert T.shortlist_regret(score3, X3, t3, prob2, 3, twins=3)[0] == 0.0
 
 
