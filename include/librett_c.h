@@ -59,6 +59,9 @@ typedef struct librett_plan_info {
   double model_cost;               /* analytic cost estimate (seconds)            */
   int selected_by;                 /* 0 analytic model, 1 learned model,
                                       2 measurement, 3 explicit candidate         */
+  int table_bytes;                 /* device offset tables the plan holds: 0 for
+                                      tiles of at most 6 ranks (addresses
+                                      computed in the kernel) and non-tile plans */
 } librett_plan_info;
 
 /* librettInitialize / librettFinalize (LibreTT src/librett.h:57,62). */
@@ -84,11 +87,14 @@ int librett_c_destroy(librettHandle handle);
  * librettPlan_t::print, src/plan.cpp:825-833). */
 int librett_c_plan_info(librettHandle handle, librett_plan_info* info);
 
-/* Device status word of a plan, read after the plan's stream has drained
- * (synchronises it): 0, or bit 0 set when a launch of the bulk-copy
- * pipeline (pipeline 3) waited longer than its limit for its copies and
- * skipped its stores.  Plans of other pipelines always read 0.  No LibreTT
- * counterpart (LibreTT exits on device errors, src/GpuUtils.h:47-56). */
+/* Device status of a plan, read after the plan's stream has drained
+ * (synchronises it): 0, or 1 when a launch of the bulk-copy pipeline
+ * (pipeline 3) waited longer than its limit for its copies and skipped its
+ * stores.  The plan's word is one of 65,536 shared device words that a
+ * timed-out launch tags with its plan; a later timeout of another plan on
+ * the same word (plans created 65,536 apart) overwrites it.  Plans of other
+ * pipelines always read 0.  No LibreTT counterpart (LibreTT exits on device
+ * errors, src/GpuUtils.h:47-56). */
 int librett_c_plan_status(librettHandle handle, unsigned* status);
 
 /* Test hook for the bulk-copy pipeline's bounded wait (no LibreTT
@@ -96,10 +102,11 @@ int librett_c_plan_status(librettHandle handle, unsigned* status);
  * 16-byte aligned) once with `extra_bytes` (1..4096) more transaction bytes
  * armed on each CTA's mbarrier than its copies deliver, so that no wait can
  * complete: every CTA gives up after its time limit (about 1 s, then up to
- * 1 s more for its copies), sets the status bit and skips its stores.
- * Synchronises the plan's stream, returns the status word the launch left in
- * *status (1 expected) and clears it; the plan stays usable.  Nothing faults:
- * the copies complete, only the armed count is never reached. */
+ * 1 s more for its copies), tags the plan's status word and skips its
+ * stores.  Synchronises the plan's stream, returns the plan's status after
+ * the launch in *status (1 expected, as librett_c_plan_status) and clears
+ * it; the plan stays usable.  Nothing faults: the copies complete, only the
+ * armed count is never reached. */
 int librett_c_bulk_wait_test(librettHandle handle, const void* idata, void* odata,
                              unsigned extra_bytes, unsigned* status);
 

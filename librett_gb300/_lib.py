@@ -41,6 +41,7 @@ class PlanInfo(ctypes.Structure):
         ("num_candidates", ctypes.c_int),
         ("model_cost", ctypes.c_double),
         ("selected_by", ctypes.c_int),
+        ("table_bytes", ctypes.c_int),
     ]
 
     def as_dict(self) -> dict:
@@ -68,6 +69,7 @@ class PlanInfo(ctypes.Structure):
             "num_candidates": self.num_candidates,
             "model_cost": self.model_cost,
             "selected_by": self.selected_by,
+            "table_bytes": self.table_bytes,
         }
 
 

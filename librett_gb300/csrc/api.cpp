@@ -134,6 +134,10 @@ void fillInfo(const lt::PlanDesc& pd, int grid, librett_plan_info* info) {
   info->candidate = pd.candidate;
   info->num_candidates = pd.numCandidates;
   info->model_cost = pd.cost;
+  if (lt::needsDeviceTables(pd)) {
+    size_t st, sm;
+    info->table_bytes = (int)lt::deviceTableBytes(pd.tile, &st, &sm);
+  }
 }
 
 void fillInfo(const PlanObj& obj, librett_plan_info* info) {
@@ -146,11 +150,12 @@ librettResult activate(librettHandle* handle, const lt::PlanDesc& pd, cudaStream
                        int sms, int selectedBy) {
   auto obj = std::make_shared<PlanObj>();
   obj->pd = pd;
+  if (pd.pipe == lt::PIPE_BULK) obj->pd.tile.statusTag = lt::nextStatusTag();
   obj->selectedBy = selectedBy;
   obj->stream = stream;
   obj->device = dev;
   obj->numSMs = sms;
-  if (lt::createDeviceTables(pd, stream, &obj->tablesAlloc, &obj->tables) != cudaSuccess)
+  if (lt::createDeviceTables(obj->pd, stream, &obj->tablesAlloc, &obj->tables) != cudaSuccess)
     return LIBRETT_INTERNAL_ERROR;
   *handle = storePlan(std::move(obj));
   return LIBRETT_SUCCESS;
@@ -300,6 +305,7 @@ librettResult librettPlanMeasure(librettHandle* handle, int rank, int* dim, int*
     int grid = 0;
     void* alloc = nullptr;
     lt::DeviceTables dt;
+    if (cands[c].pipe == lt::PIPE_BULK) cands[c].tile.statusTag = lt::nextStatusTag();
     if (!lt::finalizePlan(cands[c]) ||
         lt::createDeviceTables(cands[c], stream, &alloc, &dt) != cudaSuccess) {
       res = LIBRETT_INTERNAL_ERROR;
@@ -616,10 +622,12 @@ int librett_c_plan_status(librettHandle handle, unsigned* status) {
   if (!obj) return LIBRETT_INVALID_PLAN;
   *status = 0;
   if (obj->tables.status == nullptr) return LIBRETT_SUCCESS;
-  if (cudaMemcpyAsync(status, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+  unsigned word = 0;
+  if (cudaMemcpyAsync(&word, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
                       obj->stream) != cudaSuccess ||
       cudaStreamSynchronize(obj->stream) != cudaSuccess)
     return LIBRETT_INTERNAL_ERROR;
+  *status = word == obj->pd.tile.statusTag ? 1u : 0u;
   return LIBRETT_SUCCESS;
 }
 
@@ -635,12 +643,18 @@ int librett_c_bulk_wait_test(librettHandle handle, const void* idata, void* odat
   pd.tile.testExtraTx = (int)extra_bytes;
   int grid = 0;
   *status = 0;
+  unsigned word = 0;
   if (lt::launchPlan(pd, &obj->tables, idata, odata, obj->stream, obj->numSMs, &grid) !=
           cudaSuccess ||
-      cudaMemcpyAsync(status, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+      cudaMemcpyAsync(&word, obj->tables.status, sizeof(unsigned), cudaMemcpyDeviceToHost,
                       obj->stream) != cudaSuccess ||
-      cudaMemsetAsync(obj->tables.status, 0, sizeof(unsigned), obj->stream) != cudaSuccess ||
       cudaStreamSynchronize(obj->stream) != cudaSuccess)
+    return LIBRETT_INTERNAL_ERROR;
+  *status = word == pd.tile.statusTag ? 1u : 0u;
+  // clear the plan's word again (stream-ordered after the launch)
+  if (*status != 0 &&
+      (cudaMemsetAsync(obj->tables.status, 0, sizeof(unsigned), obj->stream) != cudaSuccess ||
+       cudaStreamSynchronize(obj->stream) != cudaSuccess))
     return LIBRETT_INTERNAL_ERROR;
   return LIBRETT_SUCCESS;
 }

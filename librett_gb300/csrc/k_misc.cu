@@ -126,9 +126,8 @@ struct TableParams {
 
 __global__ void __launch_bounds__(256)
 writeTileTablesKernel(const __grid_constant__ TableParams p, int* ldOff, int* stOff,
-                      unsigned short* stSm, unsigned* status) {
+                      unsigned short* stSm) {
   const int stride = gridDim.x * blockDim.x;
-  if (blockIdx.x == 0 && threadIdx.x == 0) *status = 0;
   for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < p.nIn; u += stride) {
     int rem = u * p.lv, off = 0;
     for (int t = 0; t < p.nTR; ++t) {
@@ -160,11 +159,7 @@ size_t deviceTableBytes(const TileParams& tp, size_t* stOffset, size_t* smOffset
   // 16-byte aligned
   *stOffset = 4 * (size_t)tp.nIn;
   *smOffset = ((4 * (size_t)(tp.nIn + tp.nOut) + 15) / 16) * 16;
-  return statusOffset(tp, *smOffset) + 16;
-}
-
-size_t statusOffset(const TileParams& tp, size_t smOffset) {
-  return ((smOffset + 2 * (size_t)tp.tileVol + 15) / 16) * 16;
+  return ((*smOffset + 2 * (size_t)tp.tileVol + 15) / 16) * 16;
 }
 
 cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStream_t s,
@@ -174,7 +169,6 @@ cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStr
   int* ld = reinterpret_cast<int*>(base);
   int* st = reinterpret_cast<int*>(base + stOffset);
   unsigned short* sm = reinterpret_cast<unsigned short*>(base + smOffset);
-  unsigned* status = reinterpret_cast<unsigned*>(base + statusOffset(tp, smOffset));
   TableParams p;
   p.tileVol = tp.tileVol;
   p.lv = tp.lv;
@@ -190,13 +184,52 @@ cudaError_t writeDeviceTables(const TileParams& tp, unsigned char* base, cudaStr
     p.trSout[t] = tp.trSout[t];
     p.trOut[t] = tp.trOut[t];
   }
-  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(p, ld, st, sm, status);
+  writeTileTablesKernel<<<(tp.tileVol + 255) / 256, 256, 0, s>>>(p, ld, st, sm);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   dt->ldOff = ld;
   dt->stOff = st;
   dt->stSm = sm;
-  dt->status = status;
+  return cudaSuccess;
+}
+
+namespace {
+
+// Status words of bulk-copy plans (zero at module load; only launches that
+// time out write to them, each with its plan's tag).
+__device__ unsigned gBulkStatus[BULK_STATUS_SLOTS];
+
+constexpr int kMaxDevices = 64;
+std::atomic<unsigned*> gBulkStatusBase[kMaxDevices];
+std::atomic<uint32_t> gStatusTag{0};
+
+}  // namespace
+
+uint32_t nextStatusTag() {
+  uint32_t t;
+  do {
+    t = gStatusTag.fetch_add(1, std::memory_order_relaxed) + 1;
+  } while (t == 0);
+  return t;
+}
+
+// The array's device address is resolved once per device (the host-side
+// symbol is only a stand-in) and kept for the life of the process; like the
+// table arena it is not supported across a cudaDeviceReset.
+cudaError_t bulkStatusWord(uint32_t tag, unsigned** word) {
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  unsigned* base = gBulkStatusBase[dev].load(std::memory_order_acquire);
+  if (base == nullptr) {
+    void* p = nullptr;
+    err = cudaGetSymbolAddress(&p, gBulkStatus);
+    if (err != cudaSuccess) return err;
+    base = static_cast<unsigned*>(p);
+    gBulkStatusBase[dev].store(base, std::memory_order_release);
+  }
+  *word = base + (tag % BULK_STATUS_SLOTS);
   return cudaSuccess;
 }
 
@@ -390,6 +423,12 @@ cudaError_t createDeviceTables(const PlanDesc& pd, cudaStream_t s, void** alloc,
   *alloc = nullptr;
   *dt = DeviceTables();
   if (pd.kernel != K_TILE || !flatTables(pd.pipe)) return cudaSuccess;
+  if (pd.pipe == PIPE_BULK) {
+    if (pd.tile.statusTag == 0) return cudaErrorInvalidValue;
+    cudaError_t err = bulkStatusWord(pd.tile.statusTag, &dt->status);
+    if (err != cudaSuccess) return err;
+  }
+  if (!needsDeviceTables(pd)) return cudaSuccess;  // table-free addressing
   size_t stOffset, smOffset;
   const size_t total = deviceTableBytes(pd.tile, &stOffset, &smOffset);
   void* d = nullptr;

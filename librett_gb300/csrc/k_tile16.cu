@@ -3,4 +3,7 @@
 #define LT_ES 16
 #define LT_LAUNCH_NAME launchTile16
 #define LT_GROUP_NAME launchGroupTile16
+#define LT_FLAT_A launchFlat16A
+#define LT_FLAT_B launchFlat16B
+#define LT_FLAT_C launchFlat16C
 #include "tile_launch.inc"

@@ -3,4 +3,7 @@
 #define LT_ES 4
 #define LT_LAUNCH_NAME launchTile4
 #define LT_GROUP_NAME launchGroupTile4
+#define LT_FLAT_A launchFlat4A
+#define LT_FLAT_B launchFlat4B
+#define LT_FLAT_C launchFlat4C
 #include "tile_launch.inc"

@@ -8,13 +8,16 @@
 // offset tables of flat-pipeline plans, so such callers use this entry
 // point instead.
 //
-// How: the flat tile kernel reads its offset tables from global memory.
-// Here those tables live in a fixed file-scope device array (every GPU that
-// loads the library holds it until the process exits).  A small kernel
-// (writeDeviceTables) writes the tables of the current problem into it, then
-// the transpose runs on them, both on the caller's stream.  Host code cannot use the array's
-// name as a device address; its address is obtained per device with
-// cudaGetSymbolAddress on the first call made with that device current.
+// How: flat and bulk-copy tiles of at most ARITH_MAX_NTR ranks compute
+// their addresses and need no tables; a bulk-copy plan's status word is a
+// slot of a static device array (bulkStatusWord).  Larger tiles read offset
+// tables from global memory; here those tables live in a fixed file-scope
+// device array (every GPU that loads the library holds it until the process
+// exits).  A small kernel (writeDeviceTables) writes the tables of the
+// current problem into it, then the transpose runs on them, both on the
+// caller's stream.  Host code cannot use the array's name as a device
+// address; its address is obtained per device with cudaGetSymbolAddress on
+// the first call made with that device current.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -99,11 +102,17 @@ extern "C" int librett_c_transpose_noalloc(int rank, const int* dim, const int* 
   }
   if (!refineCandidate(cands[pick], sms) || !finalizePlan(cands[pick]))
     return LIBRETT_INTERNAL_ERROR;
-  const PlanDesc& pd = cands[pick];
+  PlanDesc& pd = cands[pick];
   DeviceTables dt;
   const bool vecOk = ((uintptr_t)idata % 16 == 0 && (uintptr_t)odata % 16 == 0) ||
                      (pd.tile.lv == 1 && pd.tile.sv == 1);
-  if (pd.kernel == K_TILE && flatTables(pd.pipe) && vecOk) {
+  if (pd.kernel == K_TILE && pd.pipe == PIPE_BULK && vecOk) {
+    // the status word of a one-shot call has no reader; it only keeps the
+    // timed-out path of the kernel well defined
+    pd.tile.statusTag = nextStatusTag();
+    if (bulkStatusWord(pd.tile.statusTag, &dt.status) != cudaSuccess) return LIBRETT_INTERNAL_ERROR;
+  }
+  if (needsDeviceTables(pd) && vecOk) {
     size_t stOffset, smOffset;
     if (deviceTableBytes(pd.tile, &stOffset, &smOffset) > kScratchBytes)
       return LIBRETT_INVALID_PARAMETER;  // tables exceed the scratch

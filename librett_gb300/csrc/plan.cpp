@@ -553,6 +553,14 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   int k = 0;
   for (int i = 0; i < f.rank; ++i)
     if (trOfRank[f.perm[i]] >= 0) tp.trOut[k++] = trOfRank[f.perm[i]];
+  for (int t = 0; t < nTR; ++t) {
+    tp.trMul[t] = (uint32_t)(((uint64_t(1) << 32) + tp.trE[t] - 1) / tp.trE[t]);
+    const int o = tp.trOut[t];
+    tp.toE[t] = tp.trE[o];
+    tp.toSout[t] = tp.trSout[o];
+    tp.toInTile[t] = tp.trInTile[o];
+  }
+  for (int t = 0; t < nTR; ++t) tp.toMul[t] = tp.trMul[tp.trOut[t]];
   // Grid ranks, decoded in output order so that consecutive tiles write
   // neighbouring output; except that the first input grid rank goes first
   // when it has at most kInputFirstChunks chunks (and fewer than the first
@@ -603,6 +611,7 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   if (sv > 1 && unitFor(f, e, true) < sv) sv = 1;
   tp.lv = lv;
   tp.sv = sv;
+  tp.storeStraddle = nTR > 0 && tp.toE[0] % sv != 0;
   tp.padLog = log2i(lv);
   tp.nIn = tp.tileVol / lv;
   tp.nOut = tp.tileVol / sv;

@@ -99,6 +99,13 @@ struct Fused {
   int64_t sout[MAXR]; // output stride of input rank r (elements)
 };
 
+// Tiles of at most this many ranks address their units arithmetically in
+// the flat and bulk-copy kernels (no offset tables).
+constexpr int ARITH_MAX_NTR = 6;
+
+struct TileParams;
+inline int arithRanks(const TileParams& tp);
+
 // Tile-kernel parameters (passed by value as a __grid_constant__ argument).
 struct TileParams {
   uint32_t numTiles;
@@ -118,11 +125,23 @@ struct TileParams {
   int segLen;           // PIPE_BULK: elements per bulk copy (a multiple of lv)
   int testExtraTx;      // PIPE_BULK, test hook only: bytes armed on the mbarrier beyond
                         // the tile's (0; nonzero makes the bounded wait run out)
+  uint32_t statusTag;   // PIPE_BULK: nonzero tag of the plan, written to its status
+                        // word by a launch whose copies did not arrive in time
   int trE[MAXR];        // extent of tile rank t
   int trInTile[MAXR];   // in-tile input-order stride of tile rank t
   int trSin[MAXR];      // global input stride of tile rank t (elements)
   int trSout[MAXR];     // global output stride of tile rank t (elements)
   int trOut[MAXR];      // tile ranks in output order (indices into tr*)
+  // Table-free addressing (tiles of at most ARITH_MAX_NTR ranks): digit t of
+  // an in-tile index x (< 2^16) is __umulhi(x, trMul[t]) with trMul[t] =
+  // ceil(2^32 / trE[t]) (extents are at least 2); to* are the same fields
+  // for the tile ranks in output order (to*[i] = tr*[trOut[i]]).
+  uint32_t trMul[MAXR];
+  int toE[MAXR];
+  uint32_t toMul[MAXR];
+  int toSout[MAXR];
+  int toInTile[MAXR];
+  int storeStraddle;    // a store unit's elements may cross output tile rank 0
   // Grid rank g has grDiv[g].d chunks; chunk c starts at c * extent, except
   // that the last chunk starts at dim - extent, so that every tile is full
   // (a ragged last chunk overlaps its neighbour; the overlap is written
@@ -133,6 +152,12 @@ struct TileParams {
   long long grLastIn[MAXR];   // input offset of the last chunk
   long long grLastOut[MAXR];  // output offset of the last chunk
 };
+
+// Rank count the flat and bulk-copy kernels address arithmetically (the
+// template argument NTR), 0 when the tile needs its offset tables.
+inline int arithRanks(const TileParams& tp) {
+  return tp.nTR >= 1 && tp.nTR <= ARITH_MAX_NTR ? tp.nTR : 0;
+}
 
 // Row-copy parameters (TiledCopy: input rank 0 is also output rank 0).
 struct RowParams {

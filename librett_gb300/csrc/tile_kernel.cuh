@@ -53,6 +53,40 @@ __device__ __forceinline__ int smemIndex(const TileParams& p, int j) {
   return j + ((j >> p.padShift) << p.padLog);
 }
 
+// Table-free addressing for tiles of NTR ranks (1 <= NTR <= ARITH_MAX_NTR):
+// the global input offset of input-order element j of a tile, and the global
+// output offset and the input-order index of output-order element q, from
+// their mixed-radix digits.  In-tile indices are below 2^16 and extents at
+// least 2, so the digit __umulhi(x, ceil(2^32 / extent)) is exact
+// (ceil(2^32 / e) * x / 2^32 exceeds x / e by less than x / 2^32 < 1 / e).
+template <int NTR>
+__device__ __forceinline__ int arithInOffset(const TileParams& p, uint32_t j) {
+  int off = 0;
+#pragma unroll
+  for (int t = 0; t + 1 < NTR; ++t) {
+    const uint32_t q = __umulhi(j, p.trMul[t]);
+    off += (int)(j - q * (uint32_t)p.trE[t]) * p.trSin[t];
+    j = q;
+  }
+  return off + (int)j * p.trSin[NTR - 1];
+}
+
+template <int NTR>
+__device__ __forceinline__ void arithOut(const TileParams& p, uint32_t q, int& off, int& jj) {
+  off = 0;
+  jj = 0;
+#pragma unroll
+  for (int i = 0; i + 1 < NTR; ++i) {
+    const uint32_t d = __umulhi(q, p.toMul[i]);
+    const int c = (int)(q - d * (uint32_t)p.toE[i]);
+    off += c * p.toSout[i];
+    jj += c * p.toInTile[i];
+    q = d;
+  }
+  off += (int)q * p.toSout[NTR - 1];
+  jj += (int)q * p.toInTile[NTR - 1];
+}
+
 __device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
 }
@@ -255,6 +289,76 @@ __device__ __forceinline__ void storeTileFlat(const TileParams& p, const int* __
     storeUnit<ES, SV>(s, loadSmIdx<SV>(stSm, w), outBase + stOff[w]);
 }
 
+// Store unit at output-order element q (SV consecutive elements), global
+// offset off and first input-order index jj, addressed arithmetically: the
+// unit's elements step along output tile rank 0 unless the unit crosses it
+// (p.storeStraddle), then each element is decoded.
+template <int ES, int SV, int NTR>
+__device__ __forceinline__ void storeUnitArith(const TileParams& p,
+                                               const typename Word<ES>::T* s, uint32_t q,
+                                               int off, int jj, typename Word<ES>::T* outBase) {
+  using T = typename Word<ES>::T;
+  using ST = typename Word<ES * SV>::T;
+  if constexpr (SV == 1) {
+    outBase[off] = s[smemIndex(p, jj)];
+  } else {
+    T e[SV];
+    e[0] = s[smemIndex(p, jj)];
+    if (!p.storeStraddle) {
+#pragma unroll
+      for (int m = 1; m < SV; ++m) e[m] = s[smemIndex(p, jj + m * p.toInTile[0])];
+    } else {
+#pragma unroll
+      for (int m = 1; m < SV; ++m) {
+        int o2, j2;
+        arithOut<NTR>(p, q + m, o2, j2);
+        e[m] = s[smemIndex(p, j2)];
+      }
+    }
+    ST v;
+    __builtin_memcpy(&v, e, sizeof(ST));
+    *reinterpret_cast<ST*>(outBase + off) = v;
+  }
+}
+
+// Addresses of a thread's first PF store units (table-free addressing),
+// computed while the tile's loads are in flight.
+template <int NTR, int PF>
+struct ArithPrefetch {
+  int off[PF > 0 ? PF : 1];
+  int jj[PF > 0 ? PF : 1];
+
+  template <int SV>
+  __device__ __forceinline__ void load(const TileParams& p) {
+#pragma unroll
+    for (int i = 0; i < PF; ++i) {
+      const int w = threadIdx.x + i * TILE_THREADS;
+      if (w < p.nOut) arithOut<NTR>(p, (uint32_t)(w * SV), off[i], jj[i]);
+    }
+  }
+};
+
+// Store phase of the flat and bulk-copy pipelines with table-free
+// addressing: the prefetched units first, then the rest.
+template <int ES, int SV, int NTR, int PF>
+__device__ __forceinline__ void storeTileArith(const TileParams& p,
+                                               const ArithPrefetch<NTR, PF>& pf,
+                                               const typename Word<ES>::T* s,
+                                               typename Word<ES>::T* outBase) {
+#pragma unroll
+  for (int i = 0; i < PF; ++i) {
+    const int w = threadIdx.x + i * TILE_THREADS;
+    if (w < p.nOut) storeUnitArith<ES, SV, NTR>(p, s, (uint32_t)(w * SV), pf.off[i], pf.jj[i], outBase);
+  }
+  const int tv = opaque(threadIdx.x);
+#pragma unroll 4
+  for (int w = tv + PF * TILE_THREADS; w < p.nOut; w += TILE_THREADS) {
+    int off, jj;
+    arithOut<NTR>(p, (uint32_t)(w * SV), off, jj);
+    storeUnitArith<ES, SV, NTR>(p, s, (uint32_t)(w * SV), off, jj, outBase);
+  }
+}
+
 // Register-staged pipeline: load units go global -> registers -> shared
 // memory; the next tile's loads are issued before the current tile's
 // stores.  Two shared data buffers, one barrier per tile.
@@ -362,10 +466,12 @@ tileKernelAsync(const __grid_constant__ TileParams p, const typename Word<ES>::T
 }
 
 // Flat pipeline: one tile per CTA and no persistent loop, so the hardware
-// block scheduler streams tiles through the SMs in order.  The offset tables
-// were built on the host at plan time and are read from device memory
-// (L1/L2-resident: every CTA of the launch reads the same few kilobytes).
-template <int ES, int LV, int SV, int NL>
+// block scheduler streams tiles through the SMs in order.  With NTR = 0 the
+// offset tables were written at plan time and are read from device memory
+// (L1/L2-resident: every CTA of the launch reads the same few kilobytes);
+// with NTR = 1..ARITH_MAX_NTR (the tile's rank count) every unit's offsets
+// are computed from its index instead and the table pointers are unused.
+template <int ES, int LV, int SV, int NL, int NTR>
 __global__ void __launch_bounds__(TILE_THREADS)
 tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T* __restrict__ in,
                typename Word<ES>::T* __restrict__ out, const int* __restrict__ ldOff,
@@ -376,12 +482,26 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   T* s = reinterpret_cast<T*>(smraw);
   long long bin, bout;
   decodeTile(p, blockIdx.x, bin, bout);
+  auto ldOffset = [&](int u) -> int {
+    if constexpr (NTR > 0)
+      return arithInOffset<NTR>(p, (uint32_t)(u * LV));
+    else
+      return __ldg(ldOff + u);
+  };
   // store units per thread: nOut <= NL * TILE_THREADS * LV / SV; up to two
   // are prefetched, except where the register pipeline already holds
   // NL >= 4 data words (measured slower there: C3b 2 % down)
   constexpr int NS = (NL * LV + SV - 1) / SV;
   constexpr int PF_MAX = (NL >= LT_FLAT_ASYNC_MIN_NL || NL < 4) ? 2 : 0;
-  StorePrefetch<SV, NS < PF_MAX ? NS : PF_MAX> pf;
+  constexpr int PF = NS < PF_MAX ? NS : PF_MAX;
+  StorePrefetch<SV, (NTR == 0 ? PF : 0)> pf;
+  ArithPrefetch<NTR, (NTR > 0 ? PF : 0)> apf;
+  auto prefetch = [&] {
+    if constexpr (NTR > 0)
+      apf.template load<SV>(p);
+    else
+      pf.load(p, stOff, stSm);
+  };
   if constexpr (NL >= LT_FLAT_ASYNC_MIN_NL) {
     // many load units per thread: cp.async straight into shared memory
     // instead of NL data registers per thread
@@ -390,19 +510,18 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
     for (int k = 0; k < NL; ++k) {
       const int u = threadIdx.x + k * TILE_THREADS;
       if (u < p.nIn)
-        cpAsyncUnit<ES * LV>(sBase + (uint32_t)smemIndex(p, u * LV) * ES,
-                             in + bin + __ldg(ldOff + u));
+        cpAsyncUnit<ES * LV>(sBase + (uint32_t)smemIndex(p, u * LV) * ES, in + bin + ldOffset(u));
     }
-    pf.load(p, stOff, stSm);
+    prefetch();
     cpAsyncWaitAll();
   } else {
     LT v[NL];
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int u = threadIdx.x + k * TILE_THREADS;
-      if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + __ldg(ldOff + u));
+      if (u < p.nIn) v[k] = *reinterpret_cast<const LT*>(in + bin + ldOffset(u));
     }
-    pf.load(p, stOff, stSm);
+    prefetch();
 #pragma unroll
     for (int k = 0; k < NL; ++k) {
       const int u = threadIdx.x + k * TILE_THREADS;
@@ -410,7 +529,10 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
     }
   }
   __syncthreads();
-  storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
+  if constexpr (NTR > 0)
+    storeTileArith<ES, SV>(p, apf, s, out + bout);
+  else
+    storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
 }
 
 // mbarrier and bulk-copy primitives (PTX ISA: mbarrier, cp.async.bulk).
@@ -479,9 +601,10 @@ constexpr unsigned long long BULK_WAIT_NS = 1000000000ull;  // 1 s
 // instruction, no data registers), all completing on one mbarrier that
 // thread 0 arms with the tile's byte count; every thread then waits on it
 // and the stores run as in the flat pipeline.  The wait is bounded: after
-// BULK_WAIT_NS without completion the CTA sets bit 0 of *status, waits once
-// more (bounded) for its copies in flight, and returns without storing.
-template <int ES, int LV, int SV, int NL>
+// BULK_WAIT_NS without completion the CTA writes the plan's tag p.statusTag
+// to *status, waits once more (bounded) for its copies in flight, and
+// returns without storing.
+template <int ES, int LV, int SV, int NL, int NTR>
 __global__ void __launch_bounds__(TILE_THREADS)
 tileKernelBulk(const __grid_constant__ TileParams p, const typename Word<ES>::T* __restrict__ in,
                typename Word<ES>::T* __restrict__ out, const int* __restrict__ ldOff,
@@ -507,18 +630,31 @@ tileKernelBulk(const __grid_constant__ TileParams p, const typename Word<ES>::T*
   const T* src = in + bin;
   for (int k = threadIdx.x; k < nSeg; k += TILE_THREADS) {
     const int j0 = k * L;
-    bulkLoad(sBase + (uint32_t)smemIndex(p, j0) * ES, src + __ldg(ldOff + j0 / LV), segBytes, mb);
+    int off;
+    if constexpr (NTR > 0)
+      off = arithInOffset<NTR>(p, (uint32_t)j0);
+    else
+      off = __ldg(ldOff + j0 / LV);
+    bulkLoad(sBase + (uint32_t)smemIndex(p, j0) * ES, src + off, segBytes, mb);
   }
   if (threadIdx.x == 0) mbarArriveExpectTx(mb, (uint32_t)nSeg * segBytes + (uint32_t)p.testExtraTx);
   constexpr int NS = (NL * LV + SV - 1) / SV;
-  StorePrefetch<SV, NS < 2 ? NS : 2> pf;
-  pf.load(p, stOff, stSm);
+  constexpr int PF = NS < 2 ? NS : 2;
+  StorePrefetch<SV, (NTR == 0 ? PF : 0)> pf;
+  ArithPrefetch<NTR, (NTR > 0 ? PF : 0)> apf;
+  if constexpr (NTR > 0)
+    apf.template load<SV>(p);
+  else
+    pf.load(p, stOff, stSm);
   if (!mbarWaitBounded(mb, 0, BULK_WAIT_NS)) {
-    if (threadIdx.x == 0) atomicOr(status, 1u);
+    if (threadIdx.x == 0) atomicExch(status, p.statusTag);
     mbarWaitBounded(mb, 0, BULK_WAIT_NS);  // copies in flight write this CTA's shared memory
     return;
   }
-  storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
+  if constexpr (NTR > 0)
+    storeTileArith<ES, SV>(p, apf, s, out + bout);
+  else
+    storeTileFlat<ES, SV>(p, stOff, stSm, pf, s, out + bout);
 }
 
 // p + i * scale bytes.  With a scale the compiler cannot see (opaque), the

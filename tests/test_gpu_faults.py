@@ -22,7 +22,9 @@ import librett_gb300 as L
 from librett_gb300 import _lib
 from oracle import oracle as O
 
-DIMS, PERM, ES = [37, 8, 19, 6], [2, 0, 3, 1], 8  # a tile plan with device tables
+DIMS, PERM, ES = [37, 8, 19, 6], [2, 0, 3, 1], 8  # a tile plan (addresses computed in the kernel)
+# a tile of more than 6 ranks: its plan allocates and writes offset tables
+TDIMS, TPERM, TES = [4, 2, 2, 4, 4, 3, 2, 2, 3, 2, 2], [10, 7, 1, 6, 3, 0, 4, 8, 9, 5, 2], 8
 
 
 def _data(dims, es, seed=3):
@@ -51,26 +53,28 @@ def test_fault_sites_are_validated():
 def test_plan_table_allocation_failure(cuda, disarm):
     import torch
 
-    host, inp = _data(DIMS, ES)
+    host, inp = _data(TDIMS, TES)
     out = torch.zeros_like(inp)
     s = torch.cuda.current_stream()
     lib = _lib.load()
     prev = lib.librett_c_set_plan_cache(0)
     try:
+        assert L.describe(TDIMS, TPERM, TES)["table_bytes"] > 0
         L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
         with pytest.raises(L.LibrettError) as e:
-            L.Plan(DIMS, PERM, ES, s)
+            L.Plan(TDIMS, TPERM, TES, s)
         assert e.value.code == L.LIBRETT_INTERNAL_ERROR
         L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
         with pytest.raises(L.LibrettError) as e:
-            L.Plan(DIMS, PERM, ES, s, measure=(inp.data_ptr(), out.data_ptr()))
+            L.Plan(TDIMS, TPERM, TES, s, measure=(inp.data_ptr(), out.data_ptr()))
         assert e.value.code == L.LIBRETT_INTERNAL_ERROR
         # disarmed after firing: the same calls now succeed
-        with L.Plan(DIMS, PERM, ES, s) as p:
-            assert L.METHOD_NAMES[p.info()["method"]] != "Trivial"
+        with L.Plan(TDIMS, TPERM, TES, s) as p:
+            assert p.info()["table_bytes"] > 0
             p.execute(inp.data_ptr(), out.data_ptr())
         torch.cuda.synchronize()
-        assert np.array_equal(out.cpu().numpy(), O.transpose_np(host, DIMS, PERM, ES).view(np.uint8))
+        assert np.array_equal(out.cpu().numpy(),
+                              O.transpose_np(host, TDIMS, TPERM, TES).view(np.uint8))
     finally:
         lib.librett_c_set_plan_cache(prev)
 

@@ -1,5 +1,9 @@
 """Plan tables come from a host-side arena with stream-ordered reuse.
 
+Only tiles of more than 6 ranks keep offset tables (smaller tiles compute
+their addresses in the kernel), so every problem here is a rank-9..11 one
+whose plan holds tables (checked through table_bytes).
+
 A plan destroyed while kernels that read its tables are still queued on its
 stream must keep those tables intact until the stream has passed the
 destroy: plans created meanwhile on another stream get other memory, while a
@@ -19,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _problem(dims, perm, es, seed):
+    assert L.describe(dims, perm, es)["table_bytes"] > 0, (dims, perm, es)
     host = np.random.default_rng(seed).integers(0, 256, int(np.prod(dims)) * es, dtype=np.uint8)
     return host, O.transpose_np(host, dims, perm, es).view(np.uint8)
 
@@ -28,13 +33,17 @@ def test_reuse_waits_for_the_freeing_stream(cuda):
 
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     es = 4
-    dims_a, perm_a = [512, 384, 96], [2, 0, 1]
+    dims_a, perm_a = [4, 2, 4, 2, 2, 3, 2, 4, 2, 2, 2], [9, 6, 3, 7, 1, 0, 8, 10, 5, 2, 4]
     host_a, want_a = _problem(dims_a, perm_a, es, 1)
     inp_a = torch.from_numpy(host_a).cuda()
     outs_a = [torch.zeros_like(inp_a) for _ in range(4)]
     # other problems, other tables, the same range of table sizes
-    others = [([384, 512, 96], [1, 2, 0]), ([96, 512, 384], [2, 1, 0]), ([512, 96, 384], [1, 0, 2]),
-              ([300, 200, 250], [2, 0, 1]), ([250, 300, 200], [1, 2, 0]), ([64, 64, 64, 64], [3, 1, 0, 2])]
+    others = [([2, 2, 4, 2, 2, 2, 3, 2, 4, 2, 2], [10, 6, 1, 3, 0, 8, 9, 2, 4, 7, 5]),
+              ([2, 2, 2, 2, 3, 2, 2, 2, 2, 4, 2], [2, 10, 8, 6, 1, 4, 7, 9, 5, 3, 0]),
+              ([2, 3, 2, 2, 2, 2, 2, 3, 4, 2], [9, 8, 6, 5, 7, 4, 1, 3, 0, 2]),
+              ([4, 2, 2, 2, 3, 2, 4, 4, 2, 2], [5, 6, 9, 0, 2, 1, 7, 3, 8, 4]),
+              ([4, 2, 4, 3, 2, 2, 2, 3, 3, 3], [5, 4, 7, 0, 9, 2, 6, 1, 3, 8]),
+              ([2, 2, 2, 4, 4, 2, 3, 2, 2, 2], [5, 3, 0, 7, 9, 1, 6, 2, 8, 4])]
     ins_b, wants_b = [], []
     for k, (d, p) in enumerate(others):
         h, w = _problem(d, p, es, 10 + k)
@@ -80,7 +89,9 @@ def test_freed_blocks_serve_other_streams_after_the_free(cuda):
 
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     es = 8
-    probs = [([96, 80, 70], [2, 0, 1]), ([70, 96, 80], [1, 2, 0]), ([80, 70, 96], [2, 1, 0])]
+    probs = [([4, 2, 2, 4, 4, 3, 2, 2, 3, 2, 2], [10, 7, 1, 6, 3, 0, 4, 8, 9, 5, 2]),
+             ([2, 4, 2, 2, 2, 4, 3, 2, 3, 2], [0, 6, 2, 4, 7, 5, 3, 8, 9, 1]),
+             ([2, 2, 2, 4, 2, 3, 4, 2, 2, 3, 2], [9, 3, 2, 8, 7, 1, 10, 4, 5, 0, 6])]
     data = [_problem(d, p, es, 20 + k) for k, (d, p) in enumerate(probs)]
     for rnd in range(3):
         for k, (d, p) in enumerate(probs):
@@ -95,3 +106,28 @@ def test_freed_blocks_serve_other_streams_after_the_free(cuda):
                 pl.destroy()
             s.synchronize()
             assert np.array_equal(out.cpu().numpy(), w)
+
+
+def test_small_tiles_hold_no_tables(cuda):
+    """A plan whose tile has at most 6 ranks allocates nothing from the
+    table arena and writes no tables; its first execute is correct."""
+    import torch
+
+    dims, perm, es = [512, 384, 96], [2, 0, 1], 4
+    host, want = _problem_no_tables(dims, perm, es)
+    inp = torch.from_numpy(host).cuda()
+    out = torch.zeros_like(inp)
+    s = torch.cuda.current_stream()
+    before = L.table_arena_stats()
+    with L.Plan(dims, perm, es, s) as pl:
+        assert pl.info()["table_bytes"] == 0
+        assert L.table_arena_stats() == before
+        pl.execute(inp.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), want)
+
+
+def _problem_no_tables(dims, perm, es):
+    assert L.describe(dims, perm, es)["table_bytes"] == 0
+    host = np.random.default_rng(3).integers(0, 256, int(np.prod(dims)) * es, dtype=np.uint8)
+    return host, O.transpose_np(host, dims, perm, es).view(np.uint8)

@@ -135,3 +135,13 @@ def test_fast_division_formula():
         for n in ns:
             if 0 <= n < 2 ** 31:
                 assert _fastdiv(n, d) == n // d, (n, d)
+
+
+def test_umulhi_digit_exact():
+    """The flat and bulk-copy kernels take the digits of in-tile indices
+    (< 2^16) by __umulhi(x, ceil(2^32 / e)) for extents e >= 2; exhaustive
+    over e <= 4096 (the largest tile volume) and x < 2^16."""
+    x = np.arange(1 << 16, dtype=np.uint64)
+    for e in range(2, 4097):
+        m = np.uint64(((1 << 32) + e - 1) // e)
+        assert np.array_equal((x * m) >> np.uint64(32), x // np.uint64(e)), e
