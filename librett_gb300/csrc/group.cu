@@ -140,6 +140,7 @@ struct Member {
   unsigned char* out;
   int cls;
   bool aligned16;
+  bool aligned8;
   int picked = -1;   // policy pd was chosen with (-1: none yet)
   bool separate = false;  // runs its plan's own launch
   PlanDesc pd;       // flat tile plan inside a bucket
@@ -278,6 +279,15 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     out.tile = out.tileScalar;
     out.slots = out.slotsScalar;
     out.smemBytes = out.tile.smStride * out.f.esize;
+  }
+  if (out.f.esize == 4 && (out.tile.lv < 4 || out.tile.sv < 4) && m.aligned8) {
+    // 4-byte elements: 8-byte units on the sides that cannot take 16-byte
+    // ones, when the widened units still fit the member's runs
+    PlanDesc w = out;
+    if (widenUnits8(w, m.aligned16)) {
+      const GroupRunSplit wrs = groupRunSplit(w.tile);
+      if (wrs.inRun % w.tile.lv == 0 && wrs.outRun % w.tile.sv == 0) out = w;
+    }
   }
   // the kernel's run division needs in-tile indices below 2^16 (RunDiv)
   if (out.tile.tileVol >= 65536) return false;
@@ -516,7 +526,8 @@ uint64_t batchSignature(const GroupObj& g) {
   h = fnv(h, g.members.size());
   for (const Member& m : g.members) {
     const Fused& f = m.plan->pd.f;
-    h = fnv(h, ((uint64_t)f.rank << 8) | ((uint64_t)f.esize << 1) | (m.aligned16 ? 1 : 0));
+    h = fnv(h, ((uint64_t)f.rank << 8) | ((uint64_t)f.esize << 2) | (m.aligned8 ? 2 : 0) |
+                   (m.aligned16 ? 1 : 0));
     for (int r = 0; r < f.rank; ++r) h = fnv(h, ((uint64_t)f.dim[r] << 5) | (uint64_t)f.perm[r]);
   }
   return h;
@@ -580,6 +591,7 @@ librettResult create(librettGroupHandle* handle, int count, const librettHandle*
     g->bytes += 2 * bytes;
     m.cls = memberClass(bytes, f.esize);
     m.aligned16 = (uintptr_t)m.in % 16 == 0 && (uintptr_t)m.out % 16 == 0;
+    m.aligned8 = (uintptr_t)m.in % 8 == 0 && (uintptr_t)m.out % 8 == 0;
   }
   if (!independentBuffers(*g)) return LIBRETT_INVALID_PARAMETER;
   g->signature = batchSignature(*g);

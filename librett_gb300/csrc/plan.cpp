@@ -493,12 +493,11 @@ int log2i(int x) {
   return l;
 }
 
-// Largest unit (elements) that never straddles a run boundary and stays
-// 16-byte aligned for one side (input or output order), including the
-// shifted last chunks of ragged ranks.
-int unitFor(const Fused& f, const int64_t* e, bool outputSide) {
-  const int V = 16 / f.esize;
-  if (V == 1) return 1;
+// V (elements, V * esize <= 16 bytes) when units of V elements never
+// straddle a run boundary and stay V-element aligned for one side (input or
+// output order), including the shifted last chunks of ragged ranks; else 1.
+int unitFor(const Fused& f, const int64_t* e, bool outputSide, int V) {
+  if (V <= 1) return 1;
   RunInfo ri = runOf(f, e, outputSide);
   if (ri.run % V != 0) return 1;
   if (ri.frontier >= 0) {
@@ -607,8 +606,8 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   }
   tp.nGR = nGR;
   tp.numTiles = (uint32_t)numTiles;
-  if (lv > 1 && unitFor(f, e, false) < lv) lv = 1;
-  if (sv > 1 && unitFor(f, e, true) < sv) sv = 1;
+  if (lv > 1 && unitFor(f, e, false, lv) < lv) lv = 1;
+  if (sv > 1 && unitFor(f, e, true, sv) < sv) sv = 1;
   tp.lv = lv;
   tp.sv = sv;
   tp.storeStraddle = nTR > 0 && tp.toE[0] % sv != 0;
@@ -1023,6 +1022,26 @@ std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool scree
     out[i].numCandidates = (int)out.size();
   }
   return out;
+}
+
+bool widenUnits8(PlanDesc& pd, bool aligned16) {
+  if (pd.kernel != K_TILE || pd.f.esize != 4) return false;
+  const TileParams& cur = pd.tile;
+  // 16-byte sides stay (when the pointers allow them); 4-byte sides try 8
+  const int lv = cur.lv == 4 && aligned16 ? 4 : 2;
+  const int sv = cur.sv == 4 && aligned16 ? 4 : 2;
+  TileParams geom;
+  if (!buildTileGeometry(pd.f, pd.extent, lv, sv, geom)) return false;
+  if (geom.lv <= cur.lv && geom.sv <= cur.sv) return false;
+  PlanDesc w;
+  w.f = pd.f;
+  w.targetRunBytes = pd.targetRunBytes;
+  w.maxTileBytes = pd.maxTileBytes;
+  if (!buildTile(pd.f, pd.extent, PIPE_FLAT, geom, w)) return false;
+  w.candidate = pd.candidate;
+  w.numCandidates = pd.numCandidates;
+  pd = w;
+  return true;
 }
 
 bool refineCandidate(PlanDesc& pd, int numSMs) {

@@ -230,6 +230,14 @@ void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
 // exactly the candidate a full enumeration would have built.
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool screen = false);
 bool refineCandidate(PlanDesc& pd, int numSMs);
+
+// Grouped execution, 4-byte elements: rebuilds the tile of pd (same
+// extents, flat pipeline) with 8-byte units on the sides whose layout does
+// not allow 16-byte units (or both sides when the pointers are 8- but not
+// 16-byte aligned: aligned16 false).  False, pd unchanged, when no side
+// gains.  The grouped kernel is instantiated for 4-, 8- and 16-byte units of
+// 4-byte elements; single plans use 4- or 16-byte units only.
+bool widenUnits8(PlanDesc& pd, bool aligned16);
 void setAllPipelines(bool all);
 bool allPipelines();
 

@@ -223,20 +223,27 @@ void denseReluBlocked(const float* x, int n, int in, const float* wt, const floa
   }
 }
 
-// One block of exactly n rows where registers allow (AArch64 has 32 vector
-// registers: up to 6 rows by 16 outputs, or 8 rows by 8), so no row of the
-// short list is computed twice; four rows by 16 outputs elsewhere.
+// Row blocks sized for the host's vector registers.  AArch64 (32 vector
+// registers): blocks of exactly the remaining rows up to 5 (1-2 rows by 32
+// outputs, 3-5 rows by 16), 4-row blocks before a remainder of at most 5,
+// so no row is computed twice; measured on Neoverse V2 against one block of
+// 6-8 rows: n = 6: 7.3 vs 8.6 us, n = 7: 8.2 vs 8.8, n = 8: 9.1 vs 9.9.
+// Elsewhere 4 rows by 16 outputs.  Every block sums each output in the
+// same order, so the result does not depend on the split.
 void denseRelu(const float* x, int n, int in, const float* wt, const float* b, float* y) {
 #if defined(__aarch64__)
+  while (n > 5) {
+    denseReluBlocked<4, 16>(x, 4, in, wt, b, y);
+    x += (size_t)4 * in;
+    y += (size_t)4 * MLP_HIDDEN;
+    n -= 4;
+  }
   switch (n) {
-    case 1: denseReluBlocked<1, 16>(x, n, in, wt, b, y); return;
-    case 2: denseReluBlocked<2, 16>(x, n, in, wt, b, y); return;
+    case 1: denseReluBlocked<1, 32>(x, n, in, wt, b, y); return;
+    case 2: denseReluBlocked<2, 32>(x, n, in, wt, b, y); return;
     case 3: denseReluBlocked<3, 16>(x, n, in, wt, b, y); return;
     case 4: denseReluBlocked<4, 16>(x, n, in, wt, b, y); return;
-    case 5: denseReluBlocked<5, 16>(x, n, in, wt, b, y); return;
-    case 6: denseReluBlocked<6, 16>(x, n, in, wt, b, y); return;
-    case 7: denseReluBlocked<7, 8>(x, n, in, wt, b, y); return;
-    default: denseReluBlocked<8, 8>(x, n, in, wt, b, y); return;
+    default: denseReluBlocked<5, 16>(x, n, in, wt, b, y); return;
   }
 #else
   denseReluBlocked<4, 16>(x, n, in, wt, b, y);

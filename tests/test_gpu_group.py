@@ -26,10 +26,12 @@ GAP = 64
 
 def _layout(problems, misalign):
     """Byte offsets: 256-aligned starts plus, for members flagged in
-    `misalign`, a shift by one element (4 or 8 bytes)."""
+    `misalign`, a shift by one element (4 or 8 bytes), or by the given
+    number of bytes where the flag is an int."""
     offs, total = [], 0
     for (dims, _, es), mis in zip(problems, misalign):
-        start = total + (es if mis else 0)
+        shift = mis if type(mis) is int else (es if mis else 0)
+        start = total + shift
         offs.append(start)
         nb = int(np.prod(dims)) * es
         total = (start + nb + GAP + 255) // 256 * 256
@@ -113,6 +115,29 @@ def test_group_mixed_bit_exact(cuda):
     for p in plans:
         p.destroy()
     assert L.launch_count() > before
+
+
+def test_group_f32_eight_byte_units(cuda):
+    """4-byte elements move in 8-byte units on the sides whose runs or
+    pointers allow 8 but not 16 bytes (members shifted by 8 bytes are 8- but
+    not 16-byte aligned); such buckets exist and every member is bit-exact."""
+    import torch
+
+    probs = grouped_problems(300, seed=23, log2_lo=4, log2_hi=15, sizes=(4,), max_rank=6)
+    rng = np.random.default_rng(7)
+    shifts = [8 if rng.random() < 0.3 else 0 for _ in probs]
+    b = _Batch(probs, shifts, seed=9)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream) as g:
+        units = {(k["lv"], k["sv"]) for k in g.buckets() if k["es"] == 4}
+        assert any(2 in u for u in units), units
+        assert units <= {(a, c) for a in (1, 2, 4) for c in (1, 2, 4)}, units
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
 
 
 def test_group_high_rank_member(cuda):

@@ -3,7 +3,8 @@
 On problems of the selector's distribution drawn with a seed not used in
 training, plans chosen by the learned model (the default when its weight
 file is present) must run faster than plans chosen by the analytic model,
-geomean over the problems, and must not be a large loss on any one of them.
+geomean over the problems, and must not be a large loss on any one of them
+(relative for launches of 10 us or more, absolute below).
 """
 import numpy as np
 import pytest
@@ -32,5 +33,13 @@ def test_learned_choice_beats_analytic(cuda):
     # of the best on average, the network's within 2 %); timing noise on the
     # geomean of 80 problems is about 0.2 %
     assert ratio < 0.995
-    worst = max(r["exec_ms_learned"] / r["exec_ms_analytic"] for r in rows)
-    assert worst < 1.25
+    # no large loss on any one problem: at most 25 % where the analytic pick
+    # runs 10 us or longer; below that a launch is latency-bound (the
+    # candidates of a 2^16-byte problem run 4-6 us), so the loss is bounded
+    # in time instead (3 us)
+    for r in rows:
+        la, an = r["exec_ms_learned"], r["exec_ms_analytic"]
+        if an >= 0.010:
+            assert la / an < 1.25, r
+        else:
+            assert la - an < 0.003, r
