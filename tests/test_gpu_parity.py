@@ -133,6 +133,60 @@ def test_every_candidate(cuda):
     assert big_bulk >= 2
 
 
+# (dims, perm, es, candidate) of flat (pipeline 2) and bulk-copy (3) tiles
+# of 1..7 tile ranks, with store units that cross the first output tile rank
+# and without: tiles of up to 6 ranks address their units arithmetically,
+# larger ones read offset tables
+ADDRESSING_CASES = [
+    ([10, 10, 8], [0, 2, 1], 8, 6), ([6, 9, 8, 3, 3, 6], [0, 1, 4, 3, 5, 2], 16, 10),
+    ([11, 11, 4, 8, 8, 4], [5, 0, 4, 2, 1, 3], 8, 8), ([8, 9, 4], [1, 0, 2], 4, 2),
+    ([2, 9, 8], [1, 2, 0], 4, 1), ([8, 9, 4], [1, 0, 2], 4, 3),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 11), ([9, 6, 2, 4, 9], [0, 3, 4, 2, 1], 4, 4),
+    ([10, 10, 8], [0, 2, 1], 8, 1), ([8, 9, 4], [1, 0, 2], 4, 1),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 2),
+    ([3, 4, 3, 10, 10, 7, 2], [5, 6, 1, 4, 2, 3, 0], 4, 4),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 3),
+    ([3, 4, 3, 10, 10, 7, 2], [5, 6, 1, 4, 2, 3, 0], 4, 5),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 0),
+    ([3, 4, 3, 10, 10, 7, 2], [5, 6, 1, 4, 2, 3, 0], 4, 0),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 1),
+    ([3, 4, 3, 10, 10, 7, 2], [5, 6, 1, 4, 2, 3, 0], 4, 1),
+    ([2, 3, 6, 5, 10, 7], [2, 4, 1, 3, 5, 0], 16, 10),
+    ([7, 5, 2, 2, 4, 3, 9, 4], [5, 0, 2, 3, 7, 6, 1, 4], 4, 0),
+    ([8, 5, 8, 2, 5, 3, 5, 3], [6, 1, 3, 5, 0, 7, 4, 2], 4, 1),
+    ([7, 5, 2, 2, 4, 3, 9, 4], [5, 0, 2, 3, 7, 6, 1, 4], 4, 1),
+    ([6, 2, 3, 2, 4, 7, 4], [4, 0, 3, 5, 2, 6, 1], 4, 0),
+    ([2, 4, 3, 2, 5, 8, 8], [4, 1, 6, 2, 0, 5, 3], 8, 6),
+    ([6, 2, 3, 2, 4, 7, 4], [4, 0, 3, 5, 2, 6, 1], 4, 1),
+    ([2, 4, 3, 2, 5, 8, 8], [4, 1, 6, 2, 0, 5, 3], 8, 7),
+]
+
+
+def _addressing_key(info, es):
+    ext, fp, r = info["tile_extent"], info["fused_perm"], info["fused_rank"]
+    ntr = sum(1 for e in ext[:r] if e > 1)
+    first_out = next(q for q in fp[:r] if ext[q] > 1)
+    sv = info["unit_out_bytes"] // es
+    return min(ntr, 7), info["pipeline"], sv > 1 and ext[first_out] % sv != 0
+
+
+def test_addressing_every_rank_count(cuda):
+    """Flat and bulk-copy tiles of every rank count, with and without store
+    units that cross the first output tile rank, bit-exact; tables exist
+    exactly for tiles of more than 6 ranks."""
+    rng = np.random.default_rng(13)
+    keys = set()
+    for dims, perm, es, c in ADDRESSING_CASES:
+        info = L.describe(dims, perm, es, candidate=c)
+        key = _addressing_key(info, es)
+        keys.add(key)
+        assert (info["table_bytes"] > 0) == (key[0] >= 7), (dims, perm, es, c, info["table_bytes"])
+        got = _check(dims, perm, es, rng=rng, candidate=c)
+        assert got["status"] == 0
+    assert keys == {(n, p, s) for n in range(1, 8) for p in (2, 3) for s in (False, True)} - {
+        (1, 2, True), (1, 3, True)}, keys
+
+
 def test_every_candidate_all_pipelines(cuda):
     """Candidate set 1: the persistent register-staged and cp.async
     pipelines and the bulk-copy pipeline (one cp.async.bulk per contiguous
