@@ -623,9 +623,10 @@ def grouped_leg(dev, stream, peak, steps, warmup, cpu_budget, nproblems=10000):
 
 def planning_leg(dev, stream, cases):
     """Planning latency on held-out problems of the plan-selection
-    distribution: librettPlan (learned selector, plan cache off; its device
-    tables are written asynchronously, stream-ordered before any execute, so
-    the plan is usable when the call returns) and librettPlanMeasure (which
+    distribution: librettPlan (learned selector, plan cache off; a plan of a
+    tile with at most 6 ranks holds no device tables, a larger one writes its
+    tables asynchronously, stream-ordered before any execute, so the plan is
+    usable when the call returns) and librettPlanMeasure (which
     synchronises internally), each the C-ABI call's duration, median over
     the problems; librettPlan followed by a stream synchronise as well.  Each
     entry point is timed in its own loop over the problems, as LibreTT's

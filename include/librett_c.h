@@ -216,14 +216,15 @@ int librett_c_group_create(librettGroupHandle* group, int count, const librettHa
  * tile + 4 * loads: tile 0 = plan selector's tile, 1 = largest tile within
  * 10% of the best sector efficiency, 2 = largest tile, 3 = analytic model for
  * a full device; loads 0 = through registers, 1 = cp.async into shared
- * memory.  Values 0..7. */
+ * memory (one tile per CTA), 2 = cp.async with persistent CTAs (one wave of
+ * SMs x occupancy walking the bucket's tiles).  Values 0..11. */
 int librett_c_group_create_policy(librettGroupHandle* group, int count,
                                   const librettHandle* plans, void* const* idata,
                                   void* const* odata, void* stream, const int* policy);
 int librett_c_group_tune(librettGroupHandle group);
 /* Bucket `index` (launch order) of the group's graph: shape[6] = element
  * bytes, load unit, store unit (elements), load units per thread, dynamic
- * shared memory bytes, loads (0/1 as in the policy); its members, tiles
+ * shared memory bytes, loads (0/1/2 as in the policy); its members, tiles
  * and algorithmic bytes. */
 int librett_c_group_bucket(librettGroupHandle group, int index, int* shape, int* members,
                            long long* tiles, long long* bytes);

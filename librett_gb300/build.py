@@ -24,7 +24,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "librett.so"
 
 SOURCES = ["api.cpp", "plan.cpp", "select.cpp", "k_misc.cu", "k_tile4.cu", "k_tile8.cu",
-           "k_tile16.cu", "noalloc.cu", "mlp.cu", "group.cu", "verify.cu"]
+           "k_tile16.cu", "k_group4.cu", "k_group4h.cu", "k_group8.cu", "k_group16.cu",
+           "noalloc.cu", "mlp.cu", "group.cu", "verify.cu"]
 # flat and bulk-copy tile kernels: three units per element size, by tile rank count
 SOURCES += [f"k_flat{es}_{g}.cu" for es in (4, 8, 16) for g in "abc"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -101,14 +101,14 @@ size_t runTableBytes(const TileParams& tp, const GroupRunSplit& rs, size_t off[3
 
 // Policies: policy % GP_TILES picks a member's flat tile from its
 // candidates; policy / GP_TILES picks the bucket's loads (0 registers,
-// 1 cp.async).
+// 1 cp.async, one tile per CTA; 2 cp.async with persistent CTAs).
 enum GroupPolicy {
   GP_SELECTOR = 0,  // the plan selector's choice for the tensor on its own
   GP_WIDE = 1,      // the largest tile within 10% of the best sector efficiency
   GP_WIDEST = 2,    // the largest tile
   GP_FILL = 3,      // the analytic model with the device assumed full of other work
   GP_TILES = 4,
-  GP_COUNT = 2 * GP_TILES
+  GP_COUNT = 3 * GP_TILES
 };
 constexpr int SMEM_CLASS = 4096;  // bucket shared-memory granularity (bytes)
 constexpr int STAGE_MAX = 8192;   // largest store-side table set staged in shared memory
@@ -218,11 +218,12 @@ uint64_t fnv(uint64_t h, uint64_t v) {
 }
 
 cudaError_t launchGroupBucket(int es, int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                              const GroupTile* map, uint32_t tiles, int smem, cudaStream_t s) {
+                              const GroupTile* map, uint32_t tiles, int smem, cudaStream_t s,
+                              int numSMs) {
   switch (es) {
-    case 4: return launchGroupTile4(lv, sv, nl, loads, tens, map, tiles, smem, s);
-    case 8: return launchGroupTile8(lv, sv, nl, loads, tens, map, tiles, smem, s);
-    case 16: return launchGroupTile16(lv, sv, nl, loads, tens, map, tiles, smem, s);
+    case 4: return launchGroupTile4(lv, sv, nl, loads, tens, map, tiles, smem, s, numSMs);
+    case 8: return launchGroupTile8(lv, sv, nl, loads, tens, map, tiles, smem, s, numSMs);
+    case 16: return launchGroupTile16(lv, sv, nl, loads, tens, map, tiles, smem, s, numSMs);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -490,7 +491,7 @@ librettResult build(GroupObj& g, const Policy& pol) {
         launched = launchGroupBucket(b.es, b.lv, b.sv, b.nl, b.loads,
                                      reinterpret_cast<const GroupTensor*>(base + b.tensOff),
                                      reinterpret_cast<const GroupTile*>(base + b.mapOff), b.tiles,
-                                     b.smem, side[br]) == cudaSuccess;
+                                     b.smem, side[br], g.numSMs) == cudaSuccess;
       } else {
         const Member& m = g.members[-nd.bucket - 1];
         int grid = 0;

@@ -77,13 +77,19 @@ struct GroupTableJob {
 };
 
 // Launch of one bucket's kernel (defined per element size in k_tile*.cu);
-// loads: 0 registers, 1 cp.async, 2 aligned 16-byte run reads (element-size
-// load units narrower than 16 bytes only).
+// loads: 0 registers, 1 cp.async (one tile per CTA), 2 cp.async with
+// persistent CTAs (grid = numSMs x occupancy, a grid stride over the tiles).
 cudaError_t launchGroupTile4(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                             const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
+                             const GroupTile* tiles, uint32_t numTiles, int smem,
+                             cudaStream_t s, int numSMs);
 cudaError_t launchGroupTile8(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                             const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
+                             const GroupTile* tiles, uint32_t numTiles, int smem,
+                             cudaStream_t s, int numSMs);
+cudaError_t launchGroupTile4Half(int lv, int sv, int nl, int loads, const GroupTensor* tens,
+                                 const GroupTile* tiles, uint32_t numTiles, int smem,
+                                 cudaStream_t s, int numSMs);
 cudaError_t launchGroupTile16(int lv, int sv, int nl, int loads, const GroupTensor* tens,
-                              const GroupTile* tiles, uint32_t numTiles, int smem, cudaStream_t s);
+                              const GroupTile* tiles, uint32_t numTiles, int smem,
+                              cudaStream_t s, int numSMs);
 
 }  // namespace lt

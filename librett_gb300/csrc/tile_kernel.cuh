@@ -612,7 +612,7 @@ tileKernelBulk(const __grid_constant__ TileParams p, const typename Word<ES>::T*
                unsigned* status) {
   static_assert(ES * LV == 16, "bulk copies need 16-byte load units");
   using T = typename Word<ES>::T;
-  extern __shared__ __align__(128) unsigned char smraw[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   __shared__ __align__(8) unsigned long long bar;
   T* s = reinterpret_cast<T*>(smraw);
   long long bin, bout;
@@ -760,13 +760,14 @@ __device__ __forceinline__ void stShared(uint32_t addr, const typename Word<BYTE
 // multiply-add per slot.  Byte offsets are multiply-adds by a scale the
 // compiler cannot fold into shifts.
 template <int ES, int LV, int SV, int NL, int LOADS>
-__global__ void __launch_bounds__(TILE_THREADS)
-groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restrict__ tiles) {
+__device__ __forceinline__ void groupTileBody(const GroupTensor* __restrict__ tens,
+                                              const GroupTile* __restrict__ tiles,
+                                              uint32_t tileIndex) {
   using T = typename Word<ES>::T;
   using LT = typename Word<ES * LV>::T;
   using ST = typename Word<ES * SV>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const longlong2 tile = __ldg(reinterpret_cast<const longlong2*>(tiles) + blockIdx.x);
+  const longlong2 tile = __ldg(reinterpret_cast<const longlong2*>(tiles) + tileIndex);
   const GroupTensor* g = tens + (int)(tile.x >> GROUP_TILE_SHIFT);
   const long long bin = tile.x & ((1LL << GROUP_TILE_SHIFT) - 1), bout = tile.y;
   // shared memory: [store-side run tables, when staged][tile data]
@@ -927,6 +928,23 @@ groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restric
       withTables(No{}, Yes{});
     else
       withTables(No{}, No{});
+  }
+}
+
+// One tile of a group bucket per CTA (LOADS 0: loads through registers,
+// 1: cp.async), or, with LOADS 2, persistent CTAs (grid = SMs x occupancy)
+// that walk the bucket's tile list with a grid stride, cp.async loads.
+template <int ES, int LV, int SV, int NL, int LOADS>
+__global__ void __launch_bounds__(TILE_THREADS)
+groupTileKernel(const GroupTensor* __restrict__ tens, const GroupTile* __restrict__ tiles,
+                uint32_t numTiles) {
+  if constexpr (LOADS == 2) {
+    for (uint32_t t = blockIdx.x; t < numTiles; t += gridDim.x) {
+      groupTileBody<ES, LV, SV, NL, 1>(tens, tiles, t);
+      __syncthreads();  // the next tile reuses the shared buffers
+    }
+  } else {
+    groupTileBody<ES, LV, SV, NL, LOADS>(tens, tiles, blockIdx.x);
   }
 }
 

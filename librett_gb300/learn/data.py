@@ -18,9 +18,10 @@ Both datasets from the committed timings (host only; writes data.npz and
 data_large.npz):
     python -m librett_gb300.learn.data \
         --from-timings librett_gb300/models/plan_timings_gb300.npz --out data.npz
-Packing two collected datasets (base distribution, large-problem
-supplement) into a timing file of that form (host only):
-    python -m librett_gb300.learn.data --pack data.npz data_large.npz \
+Packing collected datasets (base distribution, then one or more
+large-problem supplements, merged) into a timing file of that form (host
+only):
+    python -m librett_gb300.learn.data --pack data.npz data_large.npz [more_large.npz ...] \
         --out librett_gb300/models/plan_timings_gb300.npz
 """
 from __future__ import annotations
@@ -160,6 +161,20 @@ def from_timings(path):
     return refeature(base), refeature(large)
 
 
+def merge_datasets(parts):
+    """One dataset of several collected ones (problem indices renumbered):
+    problems, candidate indices and times."""
+    problems, prob, cand, t = [], [], [], []
+    for d in parts:
+        prob.append(np.asarray(d["prob"]) + len(problems))
+        problems += json.loads(str(d["problems"]))
+        cand.append(np.asarray(d["cand"]))
+        t.append(np.asarray(d["t"]))
+    return {"problems": np.array(json.dumps(problems)), "prob": np.concatenate(prob),
+            "cand": np.concatenate(cand), "t": np.concatenate(t), "sms": parts[0]["sms"],
+            "device": parts[0]["device"]}
+
+
 def pack_timings(base, large):
     """The committed timing-file form of two collected datasets: problems,
     candidate indices and times only (features are recomputed on load)."""
@@ -180,12 +195,17 @@ def main(argv=None):
                     help="recompute features of this dataset (no GPU needed) instead of timing")
     ap.add_argument("--from-timings", default=None,
                     help="build both datasets from a committed timing file (no GPU needed)")
-    ap.add_argument("--pack", nargs=2, default=None, metavar=("BASE", "LARGE"),
-                    help="write the timing file of two collected datasets (no GPU needed)")
+    ap.add_argument("--pack", nargs="+", default=None, metavar="BASE LARGE",
+                    help="write the timing file of collected datasets: the base distribution, "
+                         "then one or more large-problem supplements, merged (no GPU needed)")
     args = ap.parse_args(argv)
     if args.pack:
-        zb, zl = np.load(args.pack[0]), np.load(args.pack[1])
-        out = pack_timings({k: zb[k] for k in zb.files}, {k: zl[k] for k in zl.files})
+        if len(args.pack) < 2:
+            ap.error("--pack needs BASE and at least one LARGE dataset")
+        zb = np.load(args.pack[0])
+        large = [np.load(f) for f in args.pack[1:]]
+        out = pack_timings({k: zb[k] for k in zb.files},
+                           merge_datasets([{k: z[k] for k in z.files} for z in large]))
         np.savez_compressed(args.out, **out)
         print(f"wrote {args.out}: {len(out['t'])} + {len(out['large_t'])} timings")
         return 0

@@ -7,7 +7,8 @@ still hold the canary.  Covered: mixed ranks, permutations and element sizes
 (4/8/16 bytes); members whose pointers are not 16-byte aligned (element
 units inside their bucket); a rank-16 member with many grid ranks; a second
 execution after the inputs changed (the graph reads the buffers anew); plans
-destroyed before the group runs; every tile policy and the autotuner; the
+destroyed before the group runs; every tile and load policy (persistent
+CTAs included) and the autotuner; the
 one-shot librettExecuteGrouped; the plain per-tensor loop; and the error
 codes.
 """
@@ -160,7 +161,9 @@ def test_group_high_rank_member(cuda):
 
 @pytest.mark.parametrize("policy", [(0, 0, 0, 0), (1, 1, 1, 1), (2, 2, 2, 2), (3, 3, 3, 3),
                                     (4, 4, 4, 4), (5, 5, 5, 5), (6, 6, 6, 6), (7, 7, 7, 7),
-                                    (2, 4, 3, 5), (6, 0, 7, 1), (7, 1, 4, 2)])
+                                    (8, 8, 8, 8), (9, 9, 9, 9), (10, 10, 10, 10),
+                                    (11, 11, 11, 11), (2, 4, 3, 5), (6, 0, 7, 1), (7, 1, 4, 2),
+                                    (10, 1, 6, 11)])
 def test_group_policies(cuda, policy):
     import torch
 
@@ -304,7 +307,7 @@ def test_group_errors(cuda):
     assert lib.librett_c_group_tune(987654) == L.LIBRETT_INVALID_PLAN
     with L.Plan([8, 16], [1, 0], 4, s) as p:
         with pytest.raises(L.LibrettError) as e:
-            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 8, 0))
+            L.Group([p], [buf.data_ptr()], [out.data_ptr()], s, policy=(0, 0, 12, 0))
         assert e.value.code == L.LIBRETT_INVALID_PARAMETER
 
 
