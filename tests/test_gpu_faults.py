@@ -23,7 +23,8 @@ from librett_gb300 import _lib
 from oracle import oracle as O
 
 DIMS, PERM, ES = [37, 8, 19, 6], [2, 0, 3, 1], 8  # a tile plan (addresses computed in the kernel)
-# a tile of more than 6 ranks: its plan allocates and writes offset tables
+# candidates with tiles of more than 6 ranks: their plans allocate and write
+# offset tables
 TDIMS, TPERM, TES = [4, 2, 2, 4, 4, 3, 2, 2, 3, 2, 2], [10, 7, 1, 6, 3, 0, 4, 8, 9, 5, 2], 8
 
 
@@ -59,17 +60,19 @@ def test_plan_table_allocation_failure(cuda, disarm):
     lib = _lib.load()
     prev = lib.librett_c_set_plan_cache(0)
     try:
-        assert L.describe(TDIMS, TPERM, TES)["table_bytes"] > 0
+        n = L.describe(TDIMS, TPERM, TES)["num_candidates"]
+        tc = next(c for c in range(n)
+                  if L.describe(TDIMS, TPERM, TES, candidate=c)["table_bytes"] > 0)
         L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
         with pytest.raises(L.LibrettError) as e:
-            L.Plan(TDIMS, TPERM, TES, s)
+            L.Plan(TDIMS, TPERM, TES, s, candidate=tc)
         assert e.value.code == L.LIBRETT_INTERNAL_ERROR
         L.inject_fault(L.FAULT_TABLE_ALLOC, 0)
         with pytest.raises(L.LibrettError) as e:
             L.Plan(TDIMS, TPERM, TES, s, measure=(inp.data_ptr(), out.data_ptr()))
         assert e.value.code == L.LIBRETT_INTERNAL_ERROR
         # disarmed after firing: the same calls now succeed
-        with L.Plan(TDIMS, TPERM, TES, s) as p:
+        with L.Plan(TDIMS, TPERM, TES, s, candidate=tc) as p:
             assert p.info()["table_bytes"] > 0
             p.execute(inp.data_ptr(), out.data_ptr())
         torch.cuda.synchronize()

@@ -2,7 +2,7 @@
 
 Only tiles of more than 6 ranks keep offset tables (smaller tiles compute
 their addresses in the kernel), so every problem here is a rank-9..11 one
-whose plan holds tables (checked through table_bytes).
+planned with a candidate that holds tables (checked through table_bytes).
 
 A plan destroyed while kernels that read its tables are still queued on its
 stream must keep those tables intact until the stream has passed the
@@ -22,8 +22,22 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
+def _tabled(dims, perm, es):
+    """A candidate of the problem whose tile keeps offset tables (more than 6
+    tile ranks), whatever the selector would pick."""
+    n = L.describe(dims, perm, es)["num_candidates"]
+    for c in range(n):
+        if L.describe(dims, perm, es, candidate=c)["table_bytes"] > 0:
+            return c
+    raise AssertionError(("no candidate with tables", dims, perm, es))
+
+
+def _plan(dims, perm, es, stream):
+    return L.Plan(dims, perm, es, stream, candidate=_tabled(dims, perm, es))
+
+
 def _problem(dims, perm, es, seed):
-    assert L.describe(dims, perm, es)["table_bytes"] > 0, (dims, perm, es)
+    _tabled(dims, perm, es)
     host = np.random.default_rng(seed).integers(0, 256, int(np.prod(dims)) * es, dtype=np.uint8)
     return host, O.transpose_np(host, dims, perm, es).view(np.uint8)
 
@@ -57,18 +71,18 @@ def test_reuse_waits_for_the_freeing_stream(cuda):
     with torch.cuda.stream(s1):
         for _ in range(40):  # tens of milliseconds of copies ahead of the transposes
             busy_dst.copy_(busy_src)
-        plan_a = L.Plan(dims_a, perm_a, es, s1)
+        plan_a = _plan(dims_a, perm_a, es, s1)
         for k in range(16):
             plan_a.execute(inp_a.data_ptr(), outs_a[k % 4].data_ptr())
         plan_a.destroy()  # its transposes are still queued behind the copies
         # the same stream may reuse the block at once
-        plan_c = L.Plan(others[0][0], others[0][1], es, s1)
+        plan_c = _plan(others[0][0], others[0][1], es, s1)
         out_c = torch.zeros_like(ins_b[0])
         plan_c.execute(ins_b[0].data_ptr(), out_c.data_ptr())
     assert s1.query() is False, "the first stream finished too early for this test to mean anything"
     plans_b = []
     for k, (d, p) in enumerate(others):
-        pb = L.Plan(d, p, es, s2)
+        pb = _plan(d, p, es, s2)
         pb.execute(ins_b[k].data_ptr(), outs_b[k].data_ptr())
         plans_b.append(pb)
     torch.cuda.synchronize()
@@ -101,7 +115,7 @@ def test_freed_blocks_serve_other_streams_after_the_free(cuda):
             out = torch.zeros_like(inp)
             torch.cuda.synchronize()
             with torch.cuda.stream(s):
-                pl = L.Plan(d, p, es, s)
+                pl = _plan(d, p, es, s)
                 pl.execute(inp.data_ptr(), out.data_ptr())
                 pl.destroy()
             s.synchronize()
