@@ -257,6 +257,20 @@ int librett_c_group_run_check(int rank, const int* dim, const int* permutation, 
 int librett_c_bulk_check(int rank, const int* dim, const int* permutation, size_t sizeofType,
                          int num_sms, int candidate);
 
+/* librettPlan on `count` problems in order, in one call (no LibreTT
+ * counterpart): for callers that create many plans, e.g. before a grouped
+ * execution, without one foreign-function round trip each.  Problem k has
+ * rank ranks[k], element size sizes[k], and its dims and permutation at the
+ * same offset of `dims` and `perms` (the problems' arrays concatenated).
+ * handles[k] receives its plan.  With synchronize nonzero every plan is
+ * followed by a cudaStreamSynchronize of `stream` (as a driver that waits for
+ * each plan before using it).  call_us, when not null, receives the host
+ * duration of each librettPlan call (and its synchronize) in microseconds.
+ * On an error the plans already made are destroyed and the error returned. */
+int librett_c_plan_batch(int count, const int* ranks, const int* dims, const int* perms,
+                         const size_t* sizes, void* stream, int synchronize,
+                         librettHandle* handles, double* call_us);
+
 /* The plain per-tensor loop the grouped path replaces: librettExecute on
  * each (plan, idata, odata) in order, one launch each; stops at and returns
  * the first error. */

@@ -129,7 +129,7 @@ class Group:
 
     # policies per member size class (librett_c.h): tile + 4 * loads
     POLICY_SELECTOR, POLICY_WIDE, POLICY_WIDEST, POLICY_FILL = 0, 1, 2, 3
-    LOADS_REGISTERS, LOADS_ASYNC = 0, 4
+    LOADS_REGISTERS, LOADS_ASYNC, LOADS_PERSISTENT = 0, 4, 8
 
     def __init__(self, plans, idata, odata, stream=None, *, policy=None):
         n, hs, ins, outs = _handle_arrays(plans, idata, odata)
@@ -240,6 +240,27 @@ def execute_grouped(plans, idata, odata) -> None:
         raise LibrettError(rc, "librett_c_execute_grouped")
 
 
+def plan_batch(problems, stream=None, synchronize=False, timings=False):
+    """librettPlan on every (dims, permutation, sizeofType) in one C call
+    (librett_c_plan_batch): a list of Plan objects, with the host duration of
+    each plan call in microseconds when `timings` is true."""
+    n = len(problems)
+    ranks = (ctypes.c_int * n)(*[len(d) for d, _, _ in problems])
+    flat_d = [int(x) for d, _, _ in problems for x in d]
+    flat_p = [int(x) for _, p, _ in problems for x in p]
+    dims = (ctypes.c_int * max(1, len(flat_d)))(*flat_d)
+    perms = (ctypes.c_int * max(1, len(flat_p)))(*flat_p)
+    sizes = (ctypes.c_size_t * n)(*[int(es) for _, _, es in problems])
+    hs = (ctypes.c_uint * n)()
+    us = (ctypes.c_double * n)() if timings else None
+    rc = _lib.load().librett_c_plan_batch(n, ranks, dims, perms, sizes, _stream(stream),
+                                          1 if synchronize else 0, hs, us)
+    if rc != LIBRETT_SUCCESS:
+        raise LibrettError(rc, "librett_c_plan_batch")
+    plans = [Plan._adopt(h, d, p, es, stream) for h, (d, p, es) in zip(hs, problems)]
+    return (plans, list(us)) if timings else plans
+
+
 def execute_batch(plans, idata, odata) -> None:
     """The plain per-tensor loop: librettExecute on every plan in order."""
     n, hs, ins, outs = _handle_arrays(plans, idata, odata)
@@ -301,6 +322,16 @@ class Plan:
         if rc != LIBRETT_SUCCESS:
             raise LibrettError(rc, "librettPlan")
         self.handle = h
+
+    @classmethod
+    def _adopt(cls, handle: int, dim, permutation, sizeofType: int, stream=None) -> "Plan":
+        """A Plan owning an existing handle (from librett_c_plan_batch)."""
+        self = cls.__new__(cls)
+        self.dim = [int(d) for d in dim]
+        self.permutation = [int(p) for p in permutation]
+        self.sizeofType = int(sizeofType)
+        self.handle = int(handle)
+        return self
 
     def execute(self, idata: int, odata: int) -> None:
         rc = librettExecute(self.handle, idata, odata)

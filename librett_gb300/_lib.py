@@ -141,6 +141,10 @@ C_FUNCTIONS = [
     ("librett_c_bulk_check", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int), ctypes.c_size_t,
       ctypes.c_int, ctypes.c_int]),
+    ("librett_c_plan_batch", ctypes.c_int,
+     [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+      ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t), _P, ctypes.c_int,
+      ctypes.POINTER(_H), ctypes.POINTER(ctypes.c_double)]),
     ("librett_c_execute_batch", ctypes.c_int,
      [ctypes.c_int, ctypes.POINTER(_H), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     ("librett_c_group_info", ctypes.c_int,

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <list>
@@ -403,6 +404,31 @@ int librett_c_execute(librettHandle handle, const void* idata, void* odata) {
 }
 
 int librett_c_destroy(librettHandle handle) { return librettDestroy(handle); }
+
+int librett_c_plan_batch(int count, const int* ranks, const int* dims, const int* perms,
+                         const size_t* sizes, void* stream, int synchronize,
+                         librettHandle* handles, double* call_us) {
+  if (count < 0 || (count > 0 && (ranks == nullptr || dims == nullptr || perms == nullptr ||
+                                  sizes == nullptr || handles == nullptr)))
+    return LIBRETT_INVALID_PARAMETER;
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t off = 0;
+  for (int k = 0; k < count; ++k) {
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc = librett_c_plan(&handles[k], ranks[k], dims + off, perms + off, sizes[k], stream);
+    const bool planned = rc == LIBRETT_SUCCESS;
+    if (planned && synchronize && cudaStreamSynchronize(s) != cudaSuccess)
+      rc = LIBRETT_INTERNAL_ERROR;
+    const auto t1 = std::chrono::steady_clock::now();
+    if (rc != LIBRETT_SUCCESS) {
+      for (int j = 0; j < k + (planned ? 1 : 0); ++j) librettDestroy(handles[j]);
+      return rc;
+    }
+    if (call_us != nullptr) call_us[k] = std::chrono::duration<double, std::micro>(t1 - t0).count();
+    off += (size_t)(ranks[k] > 0 ? ranks[k] : 0);
+  }
+  return LIBRETT_SUCCESS;
+}
 
 int librett_c_plan_info(librettHandle handle, librett_plan_info* info) {
   if (info == nullptr) return LIBRETT_INVALID_PARAMETER;

@@ -81,3 +81,11 @@ def test_plan_and_execute_without_device_fail_cleanly():
     assert rc == L.LIBRETT_INTERNAL_ERROR
     assert L.librettExecute(123456, 0, 0) == L.LIBRETT_INVALID_PLAN
     assert L.librettDestroy(123456) == L.LIBRETT_INVALID_PLAN
+
+
+def test_plan_batch_arguments():
+    """librett_c_plan_batch refuses missing arrays before planning anything."""
+    lib = _lib.load()
+    assert lib.librett_c_plan_batch(0, None, None, None, None, None, 0, None, None) == 0
+    assert lib.librett_c_plan_batch(-1, None, None, None, None, None, 0, None, None) == 2
+    assert lib.librett_c_plan_batch(2, None, None, None, None, None, 0, None, None) == 2
