@@ -1244,7 +1244,8 @@ def run_grouped(args):
                         "classes": "size class (<64KiB, <1MiB, <16MiB, larger) + 4 x element "
                                    "size (4, 8, 16 bytes)",
                         "values": "tile (0 selector, 1 wide, 2 widest, 3 full-device model) + 4 x "
-                                  "loads (0 registers, 1 cp.async)"},
+                                  "loads (0 registers, 1 cp.async, 2 cp.async with persistent "
+                                  "CTAs)"},
         "plan_s": round(plan_s, 3),
         "group_create_s": round(create_s, 3),
         "roofline": {"bound": "hbm", "kernel": "groupTileKernel", "achieved": round(gbs, 3),
