@@ -150,7 +150,31 @@ bool offsetsFit(const Fused& f, const int64_t* e) {
 // `cur`: prefer a divisor of d (no ragged last chunk) that is a multiple of
 // the 16-byte unit V when d is, among the 96 values below `want` and within
 // 60% of it; else equal chunks.
-int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
+// Results of pickExtent for one fused problem (its callers in one
+// enumeration repeat arguments often): a small direct-mapped memo.
+struct ExtentMemo {
+  static constexpr int N = 32;
+  int64_t d[N], want[N], cur[N], e[N];
+  bool used[N] = {};
+};
+
+int64_t pickExtentUncached(int64_t d, int64_t want, int64_t cur, int V);
+
+int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V, ExtentMemo* memo) {
+  if (memo == nullptr) return pickExtentUncached(d, want, cur, V);
+  const int h = (int)((uint64_t)(d * 31 + want * 7 + cur) % ExtentMemo::N);
+  if (memo->used[h] && memo->d[h] == d && memo->want[h] == want && memo->cur[h] == cur)
+    return memo->e[h];
+  const int64_t e = pickExtentUncached(d, want, cur, V);
+  memo->used[h] = true;
+  memo->d[h] = d;
+  memo->want[h] = want;
+  memo->cur[h] = cur;
+  memo->e[h] = e;
+  return e;
+}
+
+int64_t pickExtentUncached(int64_t d, int64_t want, int64_t cur, int V) {
   int64_t lo = std::max(std::max(cur + 1, (want * 3 + 4) / 5), want - 95);
   // one descending scan: the first divisor that is a multiple of V (when
   // that is preferred), else the first divisor
@@ -182,7 +206,7 @@ int64_t pickExtent(int64_t d, int64_t want, int64_t cur, int V) {
 // The side with the shorter run grows first; a rank that cannot be covered
 // whole is cut into equal chunks so the last chunk is not a sliver.
 void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t fillVol,
-                   int64_t* e) {
+                   int64_t* e, ExtentMemo* memo = nullptr) {
   for (int r = 0; r < MAXR; ++r) e[r] = 1;
   int64_t vol = 1;
   bool blocked[2] = {false, false};
@@ -212,7 +236,8 @@ void chooseExtents(const Fused& f, int64_t targetElems, int64_t maxVol, int64_t 
     int64_t enew = std::min<int64_t>(f.dim[fr], want);
     int64_t cap = (filling ? std::min(maxVol, fillVol * 2 - 1) : maxVol) / (vol / e[fr]);
     if (enew > cap) enew = cap;
-    if (enew < f.dim[fr] && enew > e[fr]) enew = pickExtent(f.dim[fr], enew, e[fr], 16 / f.esize);
+    if (enew < f.dim[fr] && enew > e[fr])
+      enew = pickExtent(f.dim[fr], enew, e[fr], 16 / f.esize, memo);
     if (enew <= e[fr]) {
       blocked[side] = true;
       continue;
@@ -404,14 +429,33 @@ long long phaseCost(const int* addr, const bool* act, int wordsPerLane) {
         }
       }
     }
+    // Lanes whose start word is a multiple of wordsPerLane (a power of two;
+    // always so for the engine's aligned units) each touch one aligned group
+    // of wordsPerLane banks: the busiest bank's count is then the largest
+    // number of lanes in one group, one increment per lane.  Otherwise every
+    // word is counted.
     unsigned char cnt[32] = {};
     int maxPerBank = 0;
+    const int groups = 32 / wordsPerLane;
+    bool aligned = true;
     for (int l = ph; l < ph + lanesPerPhase; ++l) {
       if (!act[l]) continue;
-      for (int q = 0; q < wordsPerLane; ++q) {
-        const int bk = (addr[l] + q) & 31;
-        const int c = ++cnt[bk];
-        maxPerBank = c > maxPerBank ? c : maxPerBank;
+      if (addr[l] & (wordsPerLane - 1)) {
+        aligned = false;
+        break;
+      }
+      const int c = ++cnt[(addr[l] / wordsPerLane) & (groups - 1)];
+      maxPerBank = c > maxPerBank ? c : maxPerBank;
+    }
+    if (!aligned) {
+      std::memset(cnt, 0, sizeof(cnt));
+      maxPerBank = 0;
+      for (int l = ph; l < ph + lanesPerPhase; ++l) {
+        if (!act[l]) continue;
+        for (int q = 0; q < wordsPerLane; ++q) {
+          const int c = ++cnt[(addr[l] + q) & 31];
+          maxPerBank = c > maxPerBank ? c : maxPerBank;
+        }
       }
     }
     cost += maxPerBank;
@@ -767,12 +811,14 @@ void decodeTileHost(const TileParams& tp, uint32_t tile, int64_t& bin, int64_t& 
 // In-tile offset of element x numbered in input order (outputSide false)
 // or output order (true), input or output strides.
 int64_t inTileOffset(const TileParams& tp, int x, bool outputSide) {
-  int rem = x;
+  // digits by multiply-high (trMul), exact for in-tile indices below 2^16
+  uint32_t rem = (uint32_t)x;
   int64_t off = 0;
   for (int i = 0; i < tp.nTR; ++i) {
     const int t = outputSide ? tp.trOut[i] : i;
-    const int c = rem % tp.trE[t];
-    rem /= tp.trE[t];
+    const uint32_t q = (uint32_t)(((uint64_t)rem * tp.trMul[t]) >> 32);
+    const int c = (int)(rem - q * (uint32_t)tp.trE[t]);
+    rem = q;
     off += (int64_t)c * (outputSide ? tp.trSout[t] : tp.trSin[t]);
   }
   return off;
@@ -896,13 +942,14 @@ void appendTileCandidates(const Fused& f, int numSMs, int pipes, std::vector<Pla
   constexpr int NKNOBS = sizeof(knobs) / sizeof(knobs[0]);
   int64_t seen[NKNOBS][MAXR];  // extents already enumerated
   int nSeen = 0;
+  ExtentMemo memo;  // the element size is fixed for the problem (V)
   const int V = 16 / f.esize;
   for (auto& kb : knobs) {
     int64_t target = std::max<int64_t>(1, kb[0] / f.esize);
     int64_t maxVol = std::min<int64_t>(TILE_MAX_VOL, std::max<int64_t>(1, kb[1] / f.esize));
     int64_t fillVol = std::min<int64_t>(maxVol, kb[2] / f.esize);
     int64_t* e = seen[nSeen];
-    chooseExtents(f, target, maxVol, fillVol, e);
+    chooseExtents(f, target, maxVol, fillVol, e, &memo);
     bool dup = false;
     for (int k = 0; k < nSeen && !dup; ++k)
       dup = std::equal(e, e + f.rank, seen[k]);

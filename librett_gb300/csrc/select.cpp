@@ -20,9 +20,11 @@ float lg2(double x) { return (float)std::log2(std::max(x, 1.0)); }
 
 }  // namespace
 
-void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
-  for (int i = 0; i < NFEAT; ++i) out[i] = 0.f;
-  const Fused& f = pd.f;
+namespace {
+
+// The features that depend only on the fused problem (the same for all its
+// candidates).
+void problemFeatures(const Fused& f, float* out) {
   const double vol = (double)f.vol;
   out[0] = lg2(vol) / 32.f;
   out[1] = f.esize / 16.f;
@@ -30,6 +32,12 @@ void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   out[3] = lg2((double)f.dim[0]) / 24.f;
   out[4] = lg2((double)f.dim[f.perm[0]]) / 24.f;
   out[5] = f.perm[0] == 0 ? 1.f : 0.f;
+  out[31] = lg2(vol * f.esize) / 36.f;
+}
+
+// The rest; `out` holds the problem features already.
+void candidateFeatures(const PlanDesc& pd, int numSMs, float* out) {
+  const Fused& f = pd.f;
   out[6] = pd.kernel == K_COPY;
   out[7] = pd.kernel == K_ROW;
   out[8] = pd.kernel == K_TILE;
@@ -39,7 +47,6 @@ void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   out[17] = (pd.kernel == K_TILE ? pd.unitOutBytes : pd.unitBytes) / 16.f;
   out[18] = lg2((double)pd.numWork) / 24.f;
   out[30] = (float)std::log2(std::max(pd.cost, 1e-7) * 1e6) / 16.f;
-  out[31] = lg2(vol * f.esize) / 36.f;
   if (pd.kernel != K_TILE) return;
   const TileParams& tp = pd.tile;
   out[9] = pd.pipe == PIPE_REG;
@@ -60,6 +67,14 @@ void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   out[27] = (float)pd.effIn;
   out[28] = (float)pd.effOut;
   out[29] = (float)(pd.bankPerUnit / 8.0);
+}
+
+}  // namespace
+
+void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
+  for (int i = 0; i < NFEAT; ++i) out[i] = 0.f;
+  problemFeatures(pd.f, out);
+  candidateFeatures(pd, numSMs, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -416,9 +431,12 @@ int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* devic
   }
   if (n == 1) return order[0];
   std::vector<float> x((size_t)n * NFEAT), y(n);
+  float prob[NFEAT] = {};  // the problem's features, computed once
+  problemFeatures(cands[order[0]].f, prob);
   for (int c = 0; c < n; ++c) {
     float* xc = x.data() + (size_t)c * NFEAT;
-    planFeatures(cands[order[c]], numSMs, xc);
+    std::memcpy(xc, prob, sizeof(prob));
+    candidateFeatures(cands[order[c]], numSMs, xc);
     for (int i = 0; i < NFEAT; ++i) xc[i] = (xc[i] - gModel.mean[i]) / gModel.stdv[i];
   }
   mlpForwardBatch(gModel, x.data(), n, y.data());
