@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <climits>
 #include <cstdlib>
 #include <cmath>
 #include <cstring>
@@ -486,8 +487,11 @@ int storeSample(const TileParams& tp, int sampleUnits, int* j) {
   return n;
 }
 
+// Simulated wavefronts of the sampled load and store units at a padding.
+// The count stops once it reaches `limit` (the result is then >= limit):
+// the padding search only asks whether a padding beats the best so far.
 long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUnits,
-                     const int* jStore, int nStore) {
+                     const int* jStore, int nStore, long long limit = LLONG_MAX) {
   const int words = esize / 4;
   auto smIdx = [&](int j) { return j + ((j >> padShift) << tp.padLog); };
   int addr[32];
@@ -501,6 +505,7 @@ long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUn
       addr[l] = act[l] ? smIdx(u * tp.lv) * words : 0;
     }
     total += phaseCost(addr, act, words * tp.lv);
+    if (total >= limit) return total;
   }
   for (int base = 0; base < nStore; base += 32) {
     for (int m = 0; m < tp.sv; ++m) {
@@ -510,6 +515,7 @@ long long wavefronts(const TileParams& tp, int esize, int padShift, int sampleUn
         addr[l] = act[l] ? smIdx(jStore[(size_t)m * nStore + w]) * words : 0;
       }
       total += phaseCost(addr, act, words);
+      if (total >= limit) return total;
     }
   }
   return total;
@@ -682,9 +688,11 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
     // a bulk-copy tile keeps its input segments whole between padding gaps
     if (bulkMinElems > 0 && sh != PAD_NONE && bulkSegment(tp, sh) < bulkMinElems) continue;
     // the unpadded tile's count may be known from screening
+    // a padding that cannot beat the best so far stops counting early
     long long w = sh == PAD_NONE && noneWavefronts >= 0
                       ? noneWavefronts
-                      : wavefronts(tp, f.esize, sh, 64, jStore, nStore);
+                      : wavefronts(tp, f.esize, sh, 64, jStore, nStore,
+                                   best < 0 ? LLONG_MAX : best);
     if (best < 0 || w < best) {
       best = w;
       bestShift = sh;
