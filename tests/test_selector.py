@@ -180,3 +180,24 @@ def test_targets_relative_and_clipped():
     prob = np.array([0, 0, 0, 1, 1])
     y = T.targets(t, prob)
     assert y[0] == 0 and abs(y[1] - np.log(2)) < 1e-12 and y[2] == T.Y_CLIP and y[3] == y[4] == 0
+
+
+def test_timing_file_merges_large_sets():
+    """The committed timing file packs the base set and any number of
+    large-problem sets; problem indices of later sets are renumbered."""
+    import json
+
+    def ds(problems, prob, t):
+        return {"problems": np.array(json.dumps(problems)), "prob": np.array(prob),
+                "cand": np.array([0] * len(prob)), "t": np.array(t), "sms": np.array(152),
+                "device": np.array("d")}
+
+    a = ds([[[4, 4], [1, 0], 8]], [0, 0], [1.0, 2.0])
+    b = ds([[[8, 2], [1, 0], 4], [[3, 5], [1, 0], 16]], [0, 1, 1], [3.0, 4.0, 5.0])
+    m = D.merge_datasets([a, b])
+    assert json.loads(str(m["problems"])) == [[[4, 4], [1, 0], 8], [[8, 2], [1, 0], 4],
+                                              [[3, 5], [1, 0], 16]]
+    assert m["prob"].tolist() == [0, 0, 1, 2, 2] and m["t"].tolist() == [1.0, 2.0, 3.0, 4.0, 5.0]
+    packed = D.pack_timings(a, m)
+    assert packed["large_prob"].tolist() == [0, 0, 1, 2, 2]
+    assert packed["prob"].tolist() == [0, 0]
