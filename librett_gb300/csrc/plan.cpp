@@ -681,9 +681,12 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
   }
   tp.screened = padSearch ? 0 : 1;
   int jStore[64 * 4];  // 64 store units of at most 4 elements
-  const int nStore = storeSample(tp, 64, jStore);
+  // a screened tile stays unpadded; its bank count is simulated only when a
+  // selector asks for it (bankPerUnitOf)
+  const int nStore = padSearch ? storeSample(tp, 64, jStore) : 0;
   const int shifts[] = {PAD_NONE, 8, 7, 6, 5, 4, 3, 2};
   for (int sh : shifts) {
+    if (!padSearch) break;
     if (sh < tp.padLog || (!padSearch && sh != PAD_NONE)) continue;
     // a bulk-copy tile keeps its input segments whole between padding gaps
     if (bulkMinElems > 0 && sh != PAD_NONE && bulkSegment(tp, sh) < bulkMinElems) continue;
@@ -897,9 +900,11 @@ void modelTile(PlanDesc& pd, int numSMs) {
   // store unit, over 4 schedulers x 32 lanes per SM
   const double instPerElem = 8.0 / tp.lv / util + 6.0 / tp.sv + 2.0;
   const double tIssue = (double)f.vol * overlap * instPerElem / (numSMs * 128.0 * 1.9e9);
+  // shared wavefronts per 32 sampled accesses, or -1 when the tile's bank
+  // count has not been simulated (screened candidates: bankPerUnitOf)
   const long long wf = tp.bankWavefronts;
   const int sampled = std::min(tp.nIn, 64) + std::min(tp.nOut, 64) * tp.sv;
-  pd.bankPerUnit = sampled > 0 ? (double)wf * 32.0 / sampled : 0.0;
+  pd.bankPerUnit = wf < 0 ? -1.0 : sampled > 0 ? (double)wf * 32.0 / sampled : 0.0;
   pd.cost = std::max(std::max(tDram, tFlight), std::max(tWaves, tIssue)) + kLaunch;
   // Measured on the random-shape suite: one-tile-per-CTA launches beat the
   // persistent pipelines for most shapes at equal modelled traffic.
@@ -1097,6 +1102,36 @@ bool widenUnits8(PlanDesc& pd, bool aligned16) {
   w.numCandidates = pd.numCandidates;
   pd = w;
   return true;
+}
+
+namespace {
+
+// The screened (unpadded) tile's bank count, as a full build simulates it,
+// and the feature it gives.
+long long screenedWavefronts(const PlanDesc& pd) {
+  const TileParams& tp = pd.tile;
+  int jStore[64 * 4];
+  const int nStore = storeSample(tp, 64, jStore);
+  return wavefronts(tp, pd.f.esize, tp.padShift, 64, jStore, nStore);
+}
+
+double bankFeature(const TileParams& tp, long long wf) {
+  const int sampled = std::min(tp.nIn, 64) + std::min(tp.nOut, 64) * tp.sv;
+  return sampled > 0 ? (double)wf * 32.0 / sampled : 0.0;
+}
+
+}  // namespace
+
+double bankPerUnitOf(const PlanDesc& pd) {
+  if (pd.kernel != K_TILE || pd.bankPerUnit >= 0.0) return pd.bankPerUnit;
+  return bankFeature(pd.tile, screenedWavefronts(pd));
+}
+
+void simulateBanks(PlanDesc& pd) {
+  if (pd.kernel != K_TILE || pd.bankPerUnit >= 0.0) return;
+  const long long wf = screenedWavefronts(pd);
+  pd.tile.bankWavefronts = (int)wf;
+  pd.bankPerUnit = bankFeature(pd.tile, wf);
 }
 
 bool refineCandidate(PlanDesc& pd, int numSMs) {

@@ -199,6 +199,7 @@ struct PlanDesc {
   double effIn = 1.0, effOut = 1.0;  // useful bytes / DRAM sector bytes per side
   double overlap = 1.0;              // elements moved / volume (shifted chunks)
   double bankPerUnit = 0.0;          // shared wavefronts per 32 sampled accesses
+                                     // (-1: not simulated yet, bankPerUnitOf)
   int ctasPerSM = 0;                 // modelled occupancy
   TileParams tile{};
   TileParams tileScalar{}; // element-size units (misaligned pointers)
@@ -230,6 +231,13 @@ void fuseRanks(int rank, const int* dim, const int* perm, int esize, Fused& f);
 // exactly the candidate a full enumeration would have built.
 std::vector<PlanDesc> enumerateCandidates(const Fused& f, int numSMs, bool screen = false);
 bool refineCandidate(PlanDesc& pd, int numSMs);
+
+// Shared-memory wavefronts per 32 sampled accesses of a candidate's tile
+// (pd.bankPerUnit, a selector feature): screened candidates leave the bank
+// simulation out (bankPerUnit -1) until a selector asks for it here.
+double bankPerUnitOf(const PlanDesc& pd);
+// The same, stored in pd (pd.bankPerUnit, pd.tile.bankWavefronts).
+void simulateBanks(PlanDesc& pd);
 
 // Grouped execution, 4-byte elements: rebuilds the tile of pd (same
 // extents, flat pipeline) with 8-byte units on the sides whose layout does

@@ -35,8 +35,9 @@ void problemFeatures(const Fused& f, float* out) {
   out[31] = lg2(vol * f.esize) / 36.f;
 }
 
-// The rest; `out` holds the problem features already.
-void candidateFeatures(const PlanDesc& pd, int numSMs, float* out) {
+// The rest; `out` holds the problem features already, `bank` is the
+// candidate's bankPerUnitOf.
+void candidateFeatures(const PlanDesc& pd, int numSMs, double bank, float* out) {
   const Fused& f = pd.f;
   out[6] = pd.kernel == K_COPY;
   out[7] = pd.kernel == K_ROW;
@@ -66,7 +67,7 @@ void candidateFeatures(const PlanDesc& pd, int numSMs, float* out) {
   out[26] = (float)(pd.overlap - 1.0);
   out[27] = (float)pd.effIn;
   out[28] = (float)pd.effOut;
-  out[29] = (float)(pd.bankPerUnit / 8.0);
+  out[29] = (float)(bank / 8.0);
 }
 
 }  // namespace
@@ -74,7 +75,7 @@ void candidateFeatures(const PlanDesc& pd, int numSMs, float* out) {
 void planFeatures(const PlanDesc& pd, int numSMs, float* out) {
   for (int i = 0; i < NFEAT; ++i) out[i] = 0.f;
   problemFeatures(pd.f, out);
-  candidateFeatures(pd, numSMs, out);
+  candidateFeatures(pd, numSMs, bankPerUnitOf(pd), out);
 }
 
 // ---------------------------------------------------------------------------
@@ -391,7 +392,7 @@ int shortlistSize() {
 // only 2 tiles cost 0.4 % of throughput on one GB300, so all 4 keep them.
 constexpr int SHORTLIST_TWINS = 4;
 
-int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
+int choosePlan(std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
                bool* usedLearned) {
   if (usedLearned) *usedLearned = false;
   const int mode = selectorMode();
@@ -436,7 +437,22 @@ int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* devic
   for (int c = 0; c < n; ++c) {
     float* xc = x.data() + (size_t)c * NFEAT;
     std::memcpy(xc, prob, sizeof(prob));
-    candidateFeatures(cands[order[c]], numSMs, xc);
+    // screened variants of one tile share its unpadded geometry and so its
+    // bank count: simulate it once per tile and keep it in the candidates
+    PlanDesc& pc = cands[order[c]];
+    if (pc.kernel == K_TILE && pc.bankPerUnit < 0.0) {
+      for (int j = 0; j < c; ++j) {
+        const PlanDesc& pj = cands[order[j]];
+        if (pj.screened && pj.tile.bankWavefronts >= 0 && sameTile(order[j], order[c]) &&
+            pj.tile.padShift == pc.tile.padShift) {
+          pc.tile.bankWavefronts = pj.tile.bankWavefronts;
+          pc.bankPerUnit = pj.bankPerUnit;
+          break;
+        }
+      }
+      simulateBanks(pc);
+    }
+    candidateFeatures(pc, numSMs, pc.bankPerUnit, xc);
     for (int i = 0; i < NFEAT; ++i) xc[i] = (xc[i] - gModel.mean[i]) / gModel.stdv[i];
   }
   mlpForwardBatch(gModel, x.data(), n, y.data());

@@ -67,8 +67,10 @@ bool loadSelectorModel(const char* path, std::string* why);
 
 // The candidate to use: the learned model's argmin of predicted time when
 // it applies to a device with numSMs SMs (and, when known, this device
-// name), else chooseHeuristic.  *usedLearned tells which one decided.
-int choosePlan(const std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
+// name), else chooseHeuristic.  *usedLearned tells which one decided.  The
+// bank counts it simulates for screened short-listed candidates are kept in
+// them (simulateBanks), so refining the pick does not repeat its count.
+int choosePlan(std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
                bool* usedLearned);
 
 }  // namespace lt
