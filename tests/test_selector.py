@@ -52,6 +52,37 @@ def test_host_inference_matches_float64_oracle():
     assert np.allclose(out, ref, rtol=1e-4, atol=1e-4)
 
 
+def _predict(lib, pp, X):
+    x, xp = _fp(X)
+    out = np.zeros(len(x), dtype=np.float32)
+    assert lib.librett_c_mlp_predict_host(pp, xp, len(x),
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+    return out
+
+
+def test_host_inference_does_not_depend_on_row_grouping():
+    """The host inference leaves out hidden inputs that are zero in every row
+    of a row block; a row's prediction is bit-identical whether it is scored
+    alone or in a batch with rows of other zero patterns (near-duplicate rows,
+    like the candidates of one problem, share most of their zeros)."""
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    params = T.init_params(NF, rng)
+    params[-129:-1] *= 10
+    _, pp = _fp(params)
+    base = rng.normal(size=(8, NF))
+    X = np.concatenate([b + 0.05 * rng.normal(size=(6, NF)) for b in base]).astype(np.float32)
+    whole = _predict(lib, pp, X)
+    alone = np.array([_predict(lib, pp, X[i:i + 1])[0] for i in range(len(X))], dtype=np.float32)
+    assert np.array_equal(whole.view(np.uint32), alone.view(np.uint32))
+    for n in range(1, 10):  # the planner's short-list sizes, every block split
+        order = rng.permutation(len(X))[:n]
+        got = _predict(lib, pp, X[order])
+        assert np.array_equal(got.view(np.uint32), whole[order].view(np.uint32)), n
+    ref, _ = M.forward(params, X)
+    assert np.allclose(whole, ref, rtol=1e-4, atol=1e-4)
+
+
 def test_features_finite_and_deterministic():
     for dims, perm, es in D.problems(30, seed=3):
         n = L.describe(dims, perm, es)["num_candidates"]
