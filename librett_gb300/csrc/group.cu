@@ -271,6 +271,12 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     out = c[k];
     if (!refineCandidate(out, sms)) return false;
   }
+  // narrower units than the element size allows: one rank's extent rounded
+  // to a multiple of 2 or 16 / esize elements may give the runs wider units
+  if (m.aligned16 && out.kernel == K_TILE) {
+    PlanDesc w = out;
+    if (widenUnitsByExtents(w, sms)) out = w;
+  }
   const GroupRunSplit rs = groupRunSplit(out.tile);
   const bool unitsFit = rs.inRun % out.tile.lv == 0 && rs.outRun % out.tile.sv == 0;
   if ((!m.aligned16 || !unitsFit) && (out.tile.lv > 1 || out.tile.sv > 1)) {

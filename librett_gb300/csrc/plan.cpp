@@ -1104,6 +1104,56 @@ bool widenUnits8(PlanDesc& pd, bool aligned16) {
   return true;
 }
 
+int groupUnitWidth(const TileParams& tp) {
+  const GroupRunSplit rs = groupRunSplit(tp);
+  if (rs.inRun % tp.lv != 0 || rs.outRun % tp.sv != 0) return 2;  // element units
+  return tp.lv + tp.sv;
+}
+
+bool widenUnitsByExtents(PlanDesc& pd, int numSMs) {
+  if (pd.kernel != K_TILE) return false;
+  const Fused& f = pd.f;
+  const int V = 16 / f.esize;
+  int bestW = groupUnitWidth(pd.tile);
+  if (V <= 1 || bestW >= 2 * V) return false;
+  const int vol0 = pd.tile.tileVol;
+  PlanDesc best;
+  bool found = false;
+  int64_t e[MAXR];
+  for (int r = 0; r < f.rank; ++r) {
+    if (pd.extent[r] <= 1) continue;
+    for (int m = V; m >= 2; m /= 2) {
+      const int64_t lo = pd.extent[r] / m * m;
+      const int64_t hi = lo + m;
+      for (int64_t er : {lo, hi}) {
+        if (er < 1 || er > f.dim[r] || er == pd.extent[r]) continue;
+        for (int q = 0; q < f.rank; ++q) e[q] = pd.extent[q];
+        e[r] = er;
+        TileParams geom;
+        if (!buildTileGeometry(f, e, V, V, geom)) continue;
+        // at least 3/4 and at most 5/4 of the volume the policy picked
+        if (4LL * geom.tileVol < 3LL * vol0 || 4LL * geom.tileVol > 5LL * vol0) continue;
+        const int w = groupUnitWidth(geom);
+        if (w < bestW || (w == bestW && (!found || geom.tileVol <= best.tile.tileVol))) continue;
+        PlanDesc c;
+        c.f = f;
+        c.targetRunBytes = pd.targetRunBytes;
+        c.maxTileBytes = pd.maxTileBytes;
+        if (!buildTile(f, e, pd.pipe, geom, c)) continue;
+        best = c;
+        bestW = w;
+        found = true;
+      }
+    }
+  }
+  if (!found) return false;
+  modelTile(best, numSMs < 1 ? 1 : numSMs);
+  best.candidate = pd.candidate;
+  best.numCandidates = pd.numCandidates;
+  pd = best;
+  return true;
+}
+
 namespace {
 
 // The screened (unpadded) tile's bank count, as a full build simulates it,

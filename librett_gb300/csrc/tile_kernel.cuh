@@ -102,6 +102,14 @@ __device__ __forceinline__ void cpAsyncUnit(uint32_t dst, const void* src) {
                  : "memory");
 }
 
+// L2 prefetch size of the grouped kernel's data copies: 0 (none), 128 or 256
+// bytes (the .L2::128B / .L2::256B qualifier of cp.async).  256: the
+// 10,000-member batch 0.3 % faster than none (two interleaved runs each, one
+// box); 128 made no difference.
+#ifndef LT_GROUP_L2_PREFETCH
+#define LT_GROUP_L2_PREFETCH 256
+#endif
+
 // Flat tile kernels with at least this many load units per thread load
 // through cp.async rather than registers: 8 (measured best on the float64
 // suite: 4 is 0.1 % and register loads throughout 0.7 % slower), but 4 for
@@ -681,18 +689,26 @@ __device__ __forceinline__ P* offsetBytes(P* p, int i, int scale) {
 template <int BYTES>
 __device__ __forceinline__ void cpAsyncUnitIf(bool live, uint32_t dst, const void* src) {
   static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async unit");
+#if LT_GROUP_L2_PREFETCH == 256
+#define LT_GROUP_PF ".L2::256B"
+#elif LT_GROUP_L2_PREFETCH == 128
+#define LT_GROUP_PF ".L2::128B"
+#else
+#define LT_GROUP_PF ""
+#endif
   if constexpr (BYTES == 16)
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %2, 0;\n"
-        " @p cp.async.cg.shared.global [%0], [%1], 16;\n}\n" ::"r"(dst),
+        " @p cp.async.cg.shared.global" LT_GROUP_PF " [%0], [%1], 16;\n}\n" ::"r"(dst),
         "l"(src), "r"((int)live)
         : "memory");
   else
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %3, 0;\n"
-        " @p cp.async.ca.shared.global [%0], [%1], %2;\n}\n" ::"r"(dst),
+        " @p cp.async.ca.shared.global" LT_GROUP_PF " [%0], [%1], %2;\n}\n" ::"r"(dst),
         "l"(src), "n"(BYTES), "r"((int)live)
         : "memory");
+#undef LT_GROUP_PF
 }
 
 // Shared load where live (predicated as above); the result is undefined
