@@ -5,7 +5,9 @@ its own offset with a canary-filled gap behind it.  After the group runs,
 every tensor must equal the oracle's transpose bit for bit and every gap must
 still hold the canary.  Covered: mixed ranks, permutations and element sizes
 (4/8/16 bytes); members whose pointers are not 16-byte aligned (element
-units inside their bucket); a rank-16 member with many grid ranks; a second
+units inside their bucket); members whose tile extent the grouped planner
+rounds so that their runs take 16-byte units; a rank-16 member with many
+grid ranks; a second
 execution after the inputs changed (the graph reads the buffers anew); plans
 destroyed before the group runs; every tile and load policy (persistent
 CTAs included) and the autotuner; the
@@ -135,6 +137,27 @@ def test_group_f32_eight_byte_units(cuda):
         units = {(k["lv"], k["sv"]) for k in g.buckets() if k["es"] == 4}
         assert any(2 in u for u in units), units
         assert units <= {(a, c) for a in (1, 2, 4) for c in (1, 2, 4)}, units
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_group_extent_rounding_widens_units(cuda):
+    """8-byte elements whose picked tile has odd runs on both sides (9 x 151
+    x 3, 15 x 13 x 21): the grouped planner rounds one extent to an even
+    count (the last tile of the rank shifts back to end at the dim), so the
+    runs take 16-byte units; the outputs are bit-exact."""
+    import torch
+
+    probs = [([9, 131028, 3], [2, 1, 0], 8), ([15, 13, 102, 2], [0, 2, 1, 3], 8)]
+    b = _Batch(probs, [0, 0], seed=17)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream) as g:
+        units = {(k["es"], k["lv"], k["sv"]) for k in g.buckets()}
+        assert units == {(8, 2, 2)}, units
         g.execute()
         b.check()
     for p in plans:
