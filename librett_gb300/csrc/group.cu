@@ -272,10 +272,10 @@ bool pickTile(const Member& m, int policy, int sms, const std::string& dev, Plan
     if (!refineCandidate(out, sms)) return false;
   }
   // narrower units than the element size allows: one rank's extent rounded
-  // to a multiple of 2 or 16 / esize elements may give the runs wider units
+  // to a multiple of 2 .. 16 / esize elements may give the runs wider units
   if (m.aligned16 && out.kernel == K_TILE) {
     PlanDesc w = out;
-    if (widenUnitsByExtents(w, sms)) out = w;
+    if (widenUnitsByExtents(w, sms, m.aligned8)) out = w;
   }
   const GroupRunSplit rs = groupRunSplit(out.tile);
   const bool unitsFit = rs.inRun % out.tile.lv == 0 && rs.outRun % out.tile.sv == 0;

@@ -1104,53 +1104,86 @@ bool widenUnits8(PlanDesc& pd, bool aligned16) {
   return true;
 }
 
-int groupUnitWidth(const TileParams& tp) {
-  const GroupRunSplit rs = groupRunSplit(tp);
-  if (rs.inRun % tp.lv != 0 || rs.outRun % tp.sv != 0) return 2;  // element units
-  return tp.lv + tp.sv;
+namespace {
+
+// Units (elements per load and per store unit) the grouped kernel uses for
+// the tile with extents e: 16-byte units where the layout allows them, and
+// for 4-byte elements with 8-byte aligned pointers (eight) 8-byte units on
+// the other sides; element units on both sides when a side's units would
+// cross a run of the tile.  False when the tile does not fit the kernels.
+bool groupUnitsFor(const Fused& f, const int64_t* e, bool eight, int& lv, int& sv) {
+  const int V = 16 / f.esize;
+  TileParams g;
+  if (!buildTileGeometry(f, e, V, V, g, false)) return false;
+  lv = g.lv;
+  sv = g.sv;
+  GroupRunSplit rs = groupRunSplit(g);
+  if (rs.inRun % lv != 0 || rs.outRun % sv != 0) lv = sv = 1;
+  if (f.esize == 4 && eight && (lv < 4 || sv < 4) &&
+      buildTileGeometry(f, e, lv == 4 ? 4 : 2, sv == 4 ? 4 : 2, g, false)) {
+    rs = groupRunSplit(g);
+    if (rs.inRun % g.lv == 0 && rs.outRun % g.sv == 0 && (g.lv > lv || g.sv > sv)) {
+      lv = g.lv;
+      sv = g.sv;
+    }
+  }
+  return true;
 }
 
-bool widenUnitsByExtents(PlanDesc& pd, int numSMs) {
+// Rank of a unit pair, from the grouped kernel's measured bucket rates: the
+// narrower side first (16 + 16 > 8 + 8 ~ 16 + 8 > 16 + 4 > 8 + 4 > 4 + 4
+// bytes for 4-byte elements), then the sum.
+int unitScore(int lv, int sv) { return 16 * std::min(lv, sv) + lv + sv; }
+
+}  // namespace
+
+bool widenUnitsByExtents(PlanDesc& pd, int numSMs, bool eight) {
   if (pd.kernel != K_TILE) return false;
   const Fused& f = pd.f;
   const int V = 16 / f.esize;
-  int bestW = groupUnitWidth(pd.tile);
-  if (V <= 1 || bestW >= 2 * V) return false;
-  const int vol0 = pd.tile.tileVol;
-  PlanDesc best;
-  bool found = false;
-  int64_t e[MAXR];
+  if (V <= 1) return false;
+  int lv0, sv0;
+  if (!groupUnitsFor(f, pd.extent, eight, lv0, sv0)) return false;
+  const int score0 = unitScore(lv0, sv0);
+  if (score0 >= unitScore(V, V)) return false;
+  const int64_t vol0 = pd.tile.tileVol;
+  int bestScore = score0;
+  int64_t bestVol = 0;
+  int64_t best[MAXR], e[MAXR];
   for (int r = 0; r < f.rank; ++r) {
     if (pd.extent[r] <= 1) continue;
     for (int m = V; m >= 2; m /= 2) {
       const int64_t lo = pd.extent[r] / m * m;
-      const int64_t hi = lo + m;
-      for (int64_t er : {lo, hi}) {
+      for (int64_t er : {lo, lo + m}) {
         if (er < 1 || er > f.dim[r] || er == pd.extent[r]) continue;
         for (int q = 0; q < f.rank; ++q) e[q] = pd.extent[q];
         e[r] = er;
-        TileParams geom;
-        if (!buildTileGeometry(f, e, V, V, geom)) continue;
-        // at least 3/4 and at most 5/4 of the volume the policy picked
-        if (4LL * geom.tileVol < 3LL * vol0 || 4LL * geom.tileVol > 5LL * vol0) continue;
-        const int w = groupUnitWidth(geom);
-        if (w < bestW || (w == bestW && (!found || geom.tileVol <= best.tile.tileVol))) continue;
-        PlanDesc c;
-        c.f = f;
-        c.targetRunBytes = pd.targetRunBytes;
-        c.maxTileBytes = pd.maxTileBytes;
-        if (!buildTile(f, e, pd.pipe, geom, c)) continue;
-        best = c;
-        bestW = w;
-        found = true;
+        int64_t vol = 1;
+        for (int q = 0; q < f.rank; ++q) vol *= e[q];
+        // 3/4 to 5/4 of the volume the policy picked
+        if (4 * vol < 3 * vol0 || 4 * vol > 5 * vol0) continue;
+        int lv, sv;
+        if (!groupUnitsFor(f, e, eight, lv, sv)) continue;
+        const int sc = unitScore(lv, sv);
+        if (sc < bestScore || (sc == bestScore && vol <= bestVol)) continue;
+        bestScore = sc;
+        bestVol = vol;
+        std::copy(e, e + f.rank, best);
       }
     }
   }
-  if (!found) return false;
-  modelTile(best, numSMs < 1 ? 1 : numSMs);
-  best.candidate = pd.candidate;
-  best.numCandidates = pd.numCandidates;
-  pd = best;
+  if (bestScore == score0) return false;
+  TileParams geom;
+  if (!buildTileGeometry(f, best, V, V, geom)) return false;
+  PlanDesc c;
+  c.f = f;
+  c.targetRunBytes = pd.targetRunBytes;
+  c.maxTileBytes = pd.maxTileBytes;
+  if (!buildTile(f, best, pd.pipe, geom, c)) return false;
+  modelTile(c, numSMs < 1 ? 1 : numSMs);
+  c.candidate = pd.candidate;
+  c.numCandidates = pd.numCandidates;
+  pd = c;
   return true;
 }
 

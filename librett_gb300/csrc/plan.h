@@ -246,17 +246,14 @@ void simulateBanks(PlanDesc& pd);
 // gains.  The grouped kernel is instantiated for 4-, 8- and 16-byte units of
 // 4-byte elements; single plans use 4- or 16-byte units only.
 bool widenUnits8(PlanDesc& pd, bool aligned16);
-// Grouped execution: the elements per load unit plus the elements per store
-// unit that the grouped kernel uses for a tile (1 + 1 when either side's
-// units would cross a run of the tile).
-int groupUnitWidth(const TileParams& tp);
 // Grouped execution: a tile whose runs take wider units than pd's, made by
-// rounding one rank's extent down or up to a multiple of 2 or 16 / esize
+// rounding one rank's extent down or up to a multiple of 2 .. 16 / esize
 // elements (the last tile of a rank is shifted back to end at its dim, so
-// an extent need not divide it), with 3/4 to 5/4 of pd's volume; among
-// those the widest units, then the largest volume.  False, pd unchanged,
-// when none is wider.
-bool widenUnitsByExtents(PlanDesc& pd, int numSMs);
+// an extent need not divide it), with 3/4 to 5/4 of pd's volume.  Units are
+// the grouped kernel's (with 8-byte units for 4-byte elements when eight),
+// ranked by the narrower side, then the sum, then the volume.  False, pd
+// unchanged, when no rounding gives wider units.
+bool widenUnitsByExtents(PlanDesc& pd, int numSMs, bool eight);
 void setAllPipelines(bool all);
 bool allPipelines();
 
