@@ -91,16 +91,40 @@ __device__ __forceinline__ void cpAsync16(uint32_t dst, const void* src) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
 }
 
-// cp.async of one 4-, 8- or 16-byte unit (16 bytes bypass L1).
-template <int BYTES>
+// cp.async of one 4-, 8- or 16-byte unit (16 bytes bypass L1); PF: L2
+// prefetch size in bytes (0 none, 128 or 256: the .L2::128B / .L2::256B
+// qualifier).
+template <int BYTES, int PF = 0>
 __device__ __forceinline__ void cpAsyncUnit(uint32_t dst, const void* src) {
   static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async unit");
-  if constexpr (BYTES == 16)
+  static_assert(PF == 0 || PF == 128 || PF == 256, "L2 prefetch size");
+  if constexpr (BYTES == 16 && PF == 256)
+    asm volatile("cp.async.cg.shared.global.L2::256B [%0], [%1], 16;\n" ::"r"(dst), "l"(src)
+                 : "memory");
+  else if constexpr (BYTES == 16 && PF == 128)
+    asm volatile("cp.async.cg.shared.global.L2::128B [%0], [%1], 16;\n" ::"r"(dst), "l"(src)
+                 : "memory");
+  else if constexpr (BYTES == 16)
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst), "l"(src) : "memory");
+  else if constexpr (PF == 256)
+    asm volatile("cp.async.ca.shared.global.L2::256B [%0], [%1], %2;\n" ::"r"(dst), "l"(src),
+                 "n"(BYTES)
+                 : "memory");
+  else if constexpr (PF == 128)
+    asm volatile("cp.async.ca.shared.global.L2::128B [%0], [%1], %2;\n" ::"r"(dst), "l"(src),
+                 "n"(BYTES)
+                 : "memory");
   else
     asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(dst), "l"(src), "n"(BYTES)
                  : "memory");
 }
+
+// L2 prefetch size of the single-plan flat kernel's cp.async loads: none.
+// On the 200-problem float64 suite (three interleaved runs each, one box)
+// 256 bytes measured 0.2 % slower and 128 bytes the same as none.
+#ifndef LT_FLAT_L2_PREFETCH
+#define LT_FLAT_L2_PREFETCH 0
+#endif
 
 // L2 prefetch size of the grouped kernel's data copies: 0 (none), 128 or 256
 // bytes (the .L2::128B / .L2::256B qualifier of cp.async).  256: the
@@ -525,7 +549,8 @@ tileKernelFlat(const __grid_constant__ TileParams p, const typename Word<ES>::T*
     for (int k = 0; k < NL; ++k) {
       const int u = threadIdx.x + k * TILE_THREADS;
       if (u < p.nIn)
-        cpAsyncUnit<ES * LV>(sBase + (uint32_t)smemIndex(p, u * LV) * ES, in + bin + ldOffset(u));
+        cpAsyncUnit<ES * LV, LT_FLAT_L2_PREFETCH>(sBase + (uint32_t)smemIndex(p, u * LV) * ES,
+                                                 in + bin + ldOffset(u));
     }
     prefetch();
     cpAsyncWaitAll();
