@@ -9,8 +9,14 @@
 //             librettPlan path);
 // warm (best of 10 repeats of the same problem) and cold (once, after a
 // 64 MiB host sweep that evicts the caches), and the cold plan call followed
-// by a stream synchronize.  Then librett_c_plan_measure, cold with the
-// synchronize, on every 4th problem.  Medians are printed.
+// by a stream synchronize.  After the cold plan, its first librett_c_execute
+// and a second one are timed to completion (host clock around the call and a
+// stream synchronize), so that work deferred from planning to the first
+// execute would show as their difference.  Two controls: the first and
+// second execute of a plan made warm (no sweep), and a third execute of the
+// cold plan after another sweep (an executed plan, cold host caches).  Then
+// librett_c_plan_measure, cold with the synchronize, on every 4th problem.
+// Medians are printed.
 //
 // Build and run (from the repository root, after python -m librett_gb300.build):
 //   python -c "from librett_gb300.learn import data
@@ -79,10 +85,19 @@ int main(int argc, char** argv) {
   if (cases.empty()) return 2;
   cudaStream_t s;
   if (cudaStreamCreate(&s) != cudaSuccess) return 1;
+  size_t maxBytes = 0;
+  for (const Case& k : cases) {
+    size_t v = (size_t)k.es;
+    for (int d : k.dim) v *= (size_t)d;
+    maxBytes = std::max(maxBytes, v);
+  }
+  void *a = nullptr, *b = nullptr;
+  if (cudaMalloc(&a, maxBytes) != cudaSuccess || cudaMalloc(&b, maxBytes) != cudaSuccess) return 1;
   librett_c_set_plan_cache(0);
   for (int mode : {1, 2}) {
     librett_c_set_plan_selector(mode);
-    std::vector<double> dWarm, dCold, pWarm, pCold, pColdSync;
+    std::vector<double> dWarm, dCold, pWarm, pCold, pColdSync, exFirst, exSecond, exDelta, warmDelta,
+        sweptDelta;
     for (const Case& k : cases) {
       librett_plan_info info;
       double bd = 1e30, bp = 1e30;
@@ -111,21 +126,40 @@ int main(int argc, char** argv) {
       cudaStreamSynchronize(s);
       pCold.push_back(micros(t1, t2));
       pColdSync.push_back(micros(t1, Clock::now()));
+      double ex[2];
+      for (double& e : ex) {
+        auto t3 = Clock::now();
+        if (librett_c_execute(h, a, b) != 0 || cudaStreamSynchronize(s) != cudaSuccess) return 1;
+        e = micros(t3, Clock::now());
+      }
+      exFirst.push_back(ex[0]);
+      exSecond.push_back(ex[1]);
+      exDelta.push_back(ex[0] - ex[1]);
+      sweep();
+      auto t5 = Clock::now();
+      if (librett_c_execute(h, a, b) != 0 || cudaStreamSynchronize(s) != cudaSuccess) return 1;
+      sweptDelta.push_back(micros(t5, Clock::now()) - ex[1]);
+      librett_c_destroy(h);
+      cudaStreamSynchronize(s);
+      // control: a plan made with warm caches, its first and second execute
+      if (librett_c_plan(&h, k.rank, k.dim.data(), k.perm.data(), k.es, s) != 0) return 1;
+      cudaStreamSynchronize(s);
+      for (double& e : ex) {
+        auto t3 = Clock::now();
+        if (librett_c_execute(h, a, b) != 0 || cudaStreamSynchronize(s) != cudaSuccess) return 1;
+        e = micros(t3, Clock::now());
+      }
+      warmDelta.push_back(ex[0] - ex[1]);
       librett_c_destroy(h);
       cudaStreamSynchronize(s);
     }
-    std::printf("%s: describe warm %.1f cold %.1f | plan warm %.1f cold %.1f cold+sync %.1f us\n",
+    std::printf("%s: describe warm %.1f cold %.1f | plan warm %.1f cold %.1f cold+sync %.1f us"
+                " | first execute %.1f second %.1f first-second %.1f us | controls: warm plan"
+                " first-second %.1f, executed plan after a sweep minus second %.1f us\n",
                 mode == 1 ? "analytic" : "learned ", median(dWarm), median(dCold), median(pWarm),
-                median(pCold), median(pColdSync));
+                median(pCold), median(pColdSync), median(exFirst), median(exSecond),
+                median(exDelta), median(warmDelta), median(sweptDelta));
   }
-  size_t maxBytes = 0;
-  for (const Case& k : cases) {
-    size_t v = (size_t)k.es;
-    for (int d : k.dim) v *= (size_t)d;
-    maxBytes = std::max(maxBytes, v);
-  }
-  void *a = nullptr, *b = nullptr;
-  if (cudaMalloc(&a, maxBytes) != cudaSuccess || cudaMalloc(&b, maxBytes) != cudaSuccess) return 1;
   std::vector<double> m;
   for (size_t i = 0; i < cases.size(); i += 4) {
     const Case& k = cases[i];
