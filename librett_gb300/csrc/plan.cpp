@@ -574,7 +574,7 @@ int unitFor(const Fused& f, const int64_t* e, bool outputSide, int V) {
 // kernels' limits.
 bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TileParams& tp,
                        bool padSearch = true, long long noneWavefronts = -1,
-                       int bulkMinElems = 0) {
+                       int bulkMinElems = 0, int maxVol = TILE_MAX_VOL) {
   std::memset(&tp, 0, sizeof(tp));
   int trOfRank[MAXR];
   int nTR = 0;
@@ -591,7 +591,7 @@ bool buildTileGeometry(const Fused& f, const int64_t* e, int lv, int sv, TilePar
       trOfRank[r] = -1;
     }
   }
-  if (vol > TILE_MAX_VOL || vol < 1) return false;
+  if (vol > maxVol || vol < 1) return false;
   tp.nTR = nTR;
   tp.tileVol = (int)vol;
   int s = 1;
@@ -1184,6 +1184,49 @@ bool widenUnitsByExtents(PlanDesc& pd, int numSMs, bool eight) {
   c.candidate = pd.candidate;
   c.numCandidates = pd.numCandidates;
   pd = c;
+  return true;
+}
+
+bool groupDoubleTile(PlanDesc& pd, int numSMs) {
+  if (pd.kernel != K_TILE) return false;
+  const Fused& f = pd.f;
+  const TileParams& cur = pd.tile;
+  const int lv = cur.lv, sv = cur.sv;
+  // load units per thread stay within the kernel's 16 slots
+  if (lv < 2 || GROUP_MAX_VOL / lv > TILE_THREADS * TILE_MAX_SLOTS) return false;
+  const GroupRunSplit rs0 = groupRunSplit(cur);
+  if (rs0.inRun % lv != 0 || rs0.outRun % sv != 0) return false;
+  const double eff0 = std::min(pd.effIn, pd.effOut);
+  PlanDesc best;
+  bool found = false;
+  int64_t e[MAXR];
+  for (int r = 0; r < f.rank; ++r) {
+    if (pd.extent[r] >= f.dim[r]) continue;
+    for (int q = 0; q < f.rank; ++q) e[q] = pd.extent[q];
+    e[r] = std::min<int64_t>(2 * pd.extent[r], f.dim[r]);
+    TileParams geom;
+    if (!buildTileGeometry(f, e, lv, sv, geom, true, -1, 0, GROUP_MAX_VOL)) continue;
+    if (2 * geom.tileVol < 3 * cur.tileVol || geom.lv != lv || geom.sv != sv) continue;
+    const GroupRunSplit rs = groupRunSplit(geom);
+    if (rs.inRun % lv != 0 || rs.outRun % sv != 0) continue;
+    PlanDesc c;
+    c.f = f;
+    c.targetRunBytes = pd.targetRunBytes;
+    c.maxTileBytes = pd.maxTileBytes;
+    if (!buildTile(f, e, pd.pipe, geom, c)) continue;
+    modelTile(c, numSMs < 1 ? 1 : numSMs);
+    const double eff = std::min(c.effIn, c.effOut);
+    if (eff < 0.95 * eff0) continue;
+    if (!found || eff > std::min(best.effIn, best.effOut) ||
+        (eff == std::min(best.effIn, best.effOut) && c.tile.tileVol > best.tile.tileVol)) {
+      best = c;
+      found = true;
+    }
+  }
+  if (!found) return false;
+  best.candidate = pd.candidate;
+  best.numCandidates = pd.numCandidates;
+  pd = best;
   return true;
 }
 

@@ -254,6 +254,14 @@ bool widenUnits8(PlanDesc& pd, bool aligned16);
 // ranked by the narrower side, then the sum, then the volume.  False, pd
 // unchanged, when no rounding gives wider units.
 bool widenUnitsByExtents(PlanDesc& pd, int numSMs, bool eight);
+// Largest tile of grouped execution (elements): 32 KB of 4-byte elements.
+constexpr int GROUP_MAX_VOL = 2 * TILE_MAX_VOL;
+// Grouped execution: for a tile whose load units hold at least 2 elements, a
+// tile with one rank's extent doubled (at most its dim), up to GROUP_MAX_VOL
+// elements and 16 load units per thread, that keeps pd's units and at least
+// 95 % of its sector efficiency; the best efficiency, then the largest
+// volume.  False, pd unchanged, when none.
+bool groupDoubleTile(PlanDesc& pd, int numSMs);
 void setAllPipelines(bool all);
 bool allPipelines();
 
