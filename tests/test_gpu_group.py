@@ -6,8 +6,9 @@ every tensor must equal the oracle's transpose bit for bit and every gap must
 still hold the canary.  Covered: mixed ranks, permutations and element sizes
 (4/8/16 bytes); members whose pointers are not 16-byte aligned (element
 units inside their bucket); members whose tile extent the grouped planner
-rounds so that their runs take 16-byte units; a rank-16 member with many
-grid ranks; a second
+rounds so that their runs take 16-byte units; 4-byte members in 16-byte
+units with tiles of twice the single-plan volume; a rank-16 member with
+many grid ranks; a second
 execution after the inputs changed (the graph reads the buffers anew); plans
 destroyed before the group runs; every tile and load policy (persistent
 CTAs included) and the autotuner; the
@@ -158,6 +159,27 @@ def test_group_extent_rounding_widens_units(cuda):
     with L.Group(plans, ins, outs, stream) as g:
         units = {(k["es"], k["lv"], k["sv"]) for k in g.buckets()}
         assert units == {(8, 2, 2)}, units
+        g.execute()
+        b.check()
+    for p in plans:
+        p.destroy()
+
+
+def test_group_doubles_float32_tiles(cuda):
+    """4-byte elements in 16-byte units get tiles of up to 8192 elements
+    (8 load units per thread, 32 KB) in a group, twice the single-plan
+    limit; the outputs are bit-exact."""
+    import torch
+
+    probs = [([64, 256, 64], [2, 0, 1], 4), ([128, 96, 40], [1, 2, 0], 4),
+             ([32, 48, 20, 12], [3, 1, 0, 2], 4)]
+    b = _Batch(probs, [0, 0, 0], seed=19)
+    stream = torch.cuda.current_stream()
+    plans = _plans(probs, stream)
+    ins, outs = b.ptrs()
+    with L.Group(plans, ins, outs, stream) as g:
+        shapes = {(k["es"], k["lv"], k["sv"], k["nl"]) for k in g.buckets()}
+        assert shapes == {(4, 4, 4, 8)}, shapes
         g.execute()
         b.check()
     for p in plans:
