@@ -222,14 +222,17 @@ TILE_COLS = [8, 12, 13, 14, 15, 16, 17, 18, 30]
 
 
 SHORTLIST_TWINS = 4  # short-listed tiles that keep their bulk-copy twin
+SHORTLIST_TWIN_MIN_RUN = 1024  # ... when their input runs hold this many bytes
+RUN_IN_COL = 14  # log2(input run bytes) / 20
 
 
-def shortlist_regret(score, X, t, prob, k, twins=SHORTLIST_TWINS):
+def shortlist_regret(score, X, t, prob, k, twins=SHORTLIST_TWINS, min_run=SHORTLIST_TWIN_MIN_RUN):
     """Regret of the deployed selection, per problem: within the default
     candidate set, the lowest score among the candidates of the analytic
     model's k cheapest tiles (a tile's per-unit and bulk-copy variants count
-    once, and only the `twins` cheapest tiles keep the bulk-copy variant;
-    k <= 0: among all), against the set's measured best."""
+    once, and only the `twins` cheapest tiles keep the bulk-copy variant,
+    when their input runs hold at least `min_run` bytes; k <= 0: among all),
+    against the set's measured best."""
     default = (X[:, PIPE_REG_COL] == 0) & (X[:, PIPE_ASYNC_COL] == 0)
     reg = []
     for p in np.unique(prob):
@@ -245,7 +248,8 @@ def shortlist_regret(score, X, t, prob, k, twins=SHORTLIST_TWINS):
                     if len(tiles) == k:
                         break
                     tiles.append(key)
-                if X[i, BULK_COL] == 1 and tiles.index(key) >= twins:
+                if X[i, BULK_COL] == 1 and (tiles.index(key) >= twins or
+                                            2.0 ** (X[i, RUN_IN_COL] * 20) < min_run - 0.5):
                     continue
                 short.append(i)
             keep = np.array(short, dtype=keep.dtype)

@@ -147,8 +147,9 @@ def test_learned_used_when_loaded_and_fallback_otherwise(tmp_path, restore_selec
 def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore_selector):
     """The analytic model short-lists the candidates of its 4 cheapest tiles
     (ties by index; a tile's per-unit and bulk-copy variants count once, and
-    only the SHORTLIST_TWINS cheapest tiles keep the bulk-copy variant); the
-    learned pick is the lowest prediction among those."""
+    only the SHORTLIST_TWINS cheapest tiles keep the bulk-copy variant, when
+    their input runs hold at least SHORTLIST_TWIN_MIN_RUN bytes); the learned
+    pick is the lowest prediction among those."""
     lib = restore_selector
     path, params = _write(tmp_path, sms=152)
     assert lib.librett_c_load_plan_model(path.encode()) == 0
@@ -167,7 +168,9 @@ def test_learned_pick_is_argmin_of_predictions_over_short_list(tmp_path, restore
                 if len(tiles) == 4:
                     break
                 tiles.append(key[c])
-            if infos[c]["pipeline"] == 3 and tiles.index(key[c]) >= T.SHORTLIST_TWINS:
+            if infos[c]["pipeline"] == 3 and (
+                    tiles.index(key[c]) >= T.SHORTLIST_TWINS or
+                    2.0 ** (X[c, T.RUN_IN_COL] * 20) < T.SHORTLIST_TWIN_MIN_RUN - 0.5):
                 continue
             short.append(c)
         got = L.describe(dims, perm, es)["candidate"]
@@ -191,12 +194,18 @@ def test_shortlist_regret_rules():
     assert T.shortlist_regret(score, X, t, prob, 3)[0] == 0.5  # 2 of {0, 1, 2}: 1.5 / 1.0
     assert T.shortlist_regret(score, X, t, prob, 1)[0] == 2.0  # only 0: 3.0 / 1.0
     # a bulk-copy twin of tile 0 (same tile columns) joins the short list of 1
+    X[:, T.RUN_IN_COL] = np.log2(4096) / 20  # input runs of 4 KiB
     X2 = np.concatenate([X, X[:1]])
     X2[5, T.BULK_COL] = 1
     t2 = np.concatenate([t, [1.2]])
     score2 = np.concatenate([score, [4.5]])
     prob2 = np.zeros(6, dtype=int)
     assert abs(T.shortlist_regret(score2, X2, t2, prob2, 1)[0] - 0.2) < 1e-12
+    # ... but not when the tile's input runs are shorter than the threshold
+    X2s = X2.copy()
+    X2s[:, T.RUN_IN_COL] = np.log2(512) / 20
+    assert T.shortlist_regret(score2, X2s, t2, prob2, 1)[0] == 2.0
+    assert abs(T.shortlist_regret(score2, X2s, t2, prob2, 1, min_run=0)[0] - 0.2) < 1e-12
     # a twin of the third-cheapest tile stays off the short list
     X3 = np.concatenate([X, X[2:3]])
     X3[5, T.BULK_COL] = 1
