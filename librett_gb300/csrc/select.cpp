@@ -414,9 +414,12 @@ constexpr int SHORTLIST_TWINS = 4;
 // in the timings, bulk copies of shorter runs rarely beat their per-unit
 // twin (128-255 bytes: 18 of 3528 tiles, 16 % slower at the median; 256-511:
 // 183 of 5613).  With the model trained on every candidate, the held-out
-// regret is 2.13 % over 4.99 candidates against 2.09 % over 6.20 without
-// the rule (1,800 problems of 2^28 bytes and more: 1.02 % against 0.99 %).
-constexpr int SHORTLIST_TWIN_MIN_RUN = 1024;
+// regret is 2.16 % over 4.62 candidates against 2.09 % over 6.20 without
+// the rule and 2.13 % over 4.99 with 1 KiB (1,800 problems of 2^28 bytes
+// and more: 1.03 % against 0.99 %).  On one GB300 machine, 2 KiB against 1 KiB:
+// librettPlan 16.2-16.3 against 16.6-16.7 us, the random-shape suite
+// 0.02-0.03 % slower.
+constexpr int SHORTLIST_TWIN_MIN_RUN = 2048;
 
 int choosePlan(std::vector<PlanDesc>& cands, int numSMs, const char* deviceName,
                bool* usedLearned) {

@@ -222,7 +222,7 @@ TILE_COLS = [8, 12, 13, 14, 15, 16, 17, 18, 30]
 
 
 SHORTLIST_TWINS = 4  # short-listed tiles that keep their bulk-copy twin
-SHORTLIST_TWIN_MIN_RUN = 1024  # ... when their input runs hold this many bytes
+SHORTLIST_TWIN_MIN_RUN = 2048  # ... when their input runs hold this many bytes
 RUN_IN_COL = 14  # log2(input run bytes) / 20
 
 
